@@ -1,0 +1,275 @@
+"""Benchmark of the ISLBM periodic-hill step on GB300 (one JSON line on rank 0).
+
+Workload: the 256x128x192 hill case (streamwise NY = 256, spanwise NX = 128, wall-normal
+NZ = 192; 6.29 M nodes), Re_h = 2800, Smagorinsky C_s = 0.1, U_b = 0.05, seeded perturbed
+equilibrium start, forcing controller on. One step = one fused kernel launch over all nodes.
+  value      MLUPS of the plain FP32 step, populations resident in HBM (the two FP32
+             population buffers, 2 x 478 MB, exceed the 129 MB L2, so no flush is needed)
+  e2e        MLUPS through the C ABI from host buffers: the initial populations are uploaded
+             from host memory, and every 100 steps rho, u, v, w are read back (the reference
+             main loop's mass-check cadence), all inside the timed region
+  roofline   achieved HBM GB/s of the step kernel from the algorithmic bytes (2 x 19 x 4 B
+             per node) over the CUDA-event time per launch, against the measured copy peak
+  mixed      the same for FP16 / BF16 deviation storage (2 x 19 x 2 B per node)
+  cpu_baseline  the CPU oracle (a restatement of the reference's step) on a bounded sample
+--impl reference times that CPU path alone (all host threads) on the same workload.
+Multi-GPU: replicas only (each rank runs its own solve; value is the sum over ranks).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "lattie-boltzmann-method-note_of_paperreview_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ISLBM MLUPS & %HBM peak, mixed vs plain FP32 at stated err; serve p50/p99"
+CASE = dict(NX=128, NY=256, NZ=192, Re=2800.0, Uref=0.05, NDTFRC=100, les_cs=0.1)
+WORKLOAD = "periodic hill 256x128x192 (streamwise x spanwise x wall-normal), Re_h 2800, LES Cs 0.1, Ub 0.05"
+
+
+def measured_peak_gbs():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max((float(r[2]) for r in rows if r[2].replace(".", "").isdigit()), default=None)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def time_steps(islbm, torch, solver, steps):
+    """CUDA-event time of `steps` launches on the solver's own stream (ms)."""
+    stream = torch.cuda.ExternalStream(solver.stream_handle())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    solver.step(steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def device_run(islbm, torch, precision, steps, warmup, device):
+    p = islbm.default_params(precision=precision, device=device, **CASE)
+    with islbm.Solver(p) as s:
+        s.step(warmup)
+        s.sync()
+        ms = time_steps(islbm, torch, s, steps)
+        ok = s.healthy()
+        fields = s.fields()
+    n = CASE["NX"] * CASE["NY"] * CASE["NZ"]
+    return {"ms": ms, "mlups": n * steps / (ms * 1e-3) / 1e6, "healthy": ok, "fields": fields}
+
+
+def e2e_run(islbm, precision, steps, device, f_host):
+    """Through the C ABI with host buffers: upload state, step, read fields every 100 steps."""
+    import numpy as np
+    p = islbm.default_params(precision=precision, device=device, **CASE)
+    n = CASE["NX"] * CASE["NY"] * CASE["NZ"]
+    with islbm.Solver(p) as s:
+        s.sync()
+        t0 = time.perf_counter()
+        s.set_populations(f_host)
+        done, reads = 0, 0
+        while done < steps:
+            chunk = min(100, steps - done)
+            s.step(chunk)
+            done += chunk
+            s.fields()
+            reads += 1
+        s.sync()
+        dt = time.perf_counter() - t0
+    h2d = 19 * n * np.dtype(np.float64).itemsize
+    d2h = reads * 4 * n * 8
+    return {"value": n * steps / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d / steps,
+            "d2h_bytes_per_step": d2h / steps, "note": "FP64 host buffers through islbm_set_populations / "
+                                                       "islbm_step / islbm_fields"}
+
+
+def cpu_oracle_run(steps, threads):
+    """The CPU oracle (reference restatement) on the same workload; returns MLUPS."""
+    from oracle.oracle import Oracle
+    o = Oracle(CASE["NX"], CASE["NY"], CASE["NZ"], re=CASE["Re"], ub=CASE["Uref"], ndtfrc=CASE["NDTFRC"],
+               les_cs=CASE["les_cs"], threads=threads)
+    o.step(1)  # warm
+    t0 = time.perf_counter()
+    o.step(steps)
+    dt = time.perf_counter() - t0
+    o.close()
+    n = CASE["NX"] * CASE["NY"] * CASE["NZ"]
+    return n * steps / dt / 1e6, dt
+
+
+def rel_l2(a, b):
+    import numpy as np
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        from oracle import build as ob
+        ob.build()
+        mlups, dt = cpu_oracle_run(max(args.steps, 1), threads)
+        line = {"metric": METRIC, "value": mlups, "unit": "MLUPS", "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / max(args.steps, 1) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": WORKLOAD, "grid": "NY256 NX128 NZ192", "precision": "fp64"},
+                "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
+                                 "sample": f"{args.steps} steps of the full 256x128x192 grid"},
+                "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import numpy as np
+    import torch
+    import islbm
+    import islbm_build
+    islbm_build.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    peak, peak_kind = measured_peak_gbs()
+    n = CASE["NX"] * CASE["NY"] * CASE["NZ"]
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # plain FP32, device resident
+    barrier()
+    with ClockSampler(local) as clk:
+        r32 = device_run(islbm, torch, "fp32", args.steps, args.warmup, local)
+    barrier()
+    ms = r32["ms"]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = n * args.steps * world / (ms * 1e-3) / 1e6
+    bytes_per_launch = 2 * 19 * 4 * n
+    achieved = bytes_per_launch / (ms * 1e-3 / args.steps) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded perturbed equilibrium)",
+            "config": {"workload": WORKLOAD, "grid": "NY256 NX128 NZ192", "precision": "fp32",
+                       "l2": "inputs larger than L2 (2 x 478 MB population buffers), no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "gpu_launches": args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_model": "2 x 19 x 4 B per node per step (read + write each population once)"},
+            "clocks": clk.summary()}
+    if rank == 0 and not args.no_mixed:
+        mixed = {}
+        for prec in ("fp16", "bf16"):
+            r = device_run(islbm, torch, prec, args.steps, args.warmup, local)
+            ach = 2 * 19 * 2 * n / (r["ms"] * 1e-3 / args.steps) / 1e9
+            err_u = rel_l2(np.stack([r["fields"][c] for c in "uvw"]), np.stack([r32["fields"][c] for c in "uvw"]))
+            mixed[prec] = {"mlups": r["mlups"], "speedup_vs_fp32": r["mlups"] / r32["mlups"],
+                           "hbm_gbs": ach, "frac": ach / peak, "rel_l2_u_vs_fp32": err_u,
+                           "steps": args.steps + args.warmup}
+        line["mixed"] = mixed
+    if rank == 0 and not args.no_e2e:
+        p = islbm.default_params(precision="fp32", device=local, **CASE)
+        with islbm.Solver(p) as s:
+            f_host = s.populations()
+        line["e2e"] = e2e_run(islbm, "fp32", args.steps, local, f_host)
+    if rank == 0 and not args.no_cpu:
+        from oracle import build as ob
+        ob.build()
+        mlups, dt = cpu_oracle_run(args.cpu_steps, threads)
+        line["cpu_baseline"] = {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
+                                "sample": f"{args.cpu_steps} steps of the full 256x128x192 grid, FP64, LES",
+                                "seconds": dt}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

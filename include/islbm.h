@@ -1,0 +1,154 @@
+/* islbm.h - C ABI of the GB300 ISLBM periodic-hill step library (libislbm_gb300.so).
+ *
+ * Drop-in for the reference solver's step path (ChenPengChung/Lattie-Boltzmann-Method-Note_of_
+ * PaperReView, directory 筆記：金的code/0.可更改的code/, cited below as C/):
+ *   islbm_init    replaces AllocateMemory + GenerateMesh_X/Y/Z + GetIntrplParameter_X/Y/Xi +
+ *                 BFLInitialization + InitialUsingDftFunc + SendDataToGPU
+ *                 (C/memory.h:51, C/initialization.h:6-360, C/communication.h:245)
+ *   islbm_step    replaces n calls of Launch_CollisionStreaming(f_old, f_new) with the
+ *                 ft/fd ping-pong of the main loop, AccumulateUbulk, and
+ *                 Launch_ModifyForcingTerm every NDTFRC steps (C/evolution.h:826-1042)
+ *   islbm_fields  replaces SendDataToCPU for rho, u, v, w (C/communication.h:260-273)
+ *   islbm_destroy replaces FreeSource (C/memory.h:173)
+ * The whole domain lives on one GPU; the reference's MPI halo exchange and periodic ghost
+ * kernels are replaced by in-kernel periodic wrap.
+ *
+ * Axes and names follow the reference (C/variables.h): x = spanwise (NX, LX, periodic),
+ * y = streamwise (NY, LY, periodic, hill and body force along y), z = wall-normal (NZ, LZ,
+ * body-fitted). u, v, w are the x, y, z velocity components.
+ *
+ * Conventions: every function returns an islbm_status; no function calls exit(). Host
+ * buffers belong to the caller, device buffers to the handle. A handle owns one CUDA stream;
+ * use one handle per host thread (calls on one handle are not thread-safe).
+ */
+#ifndef ISLBM_H
+#define ISLBM_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define ISLBM_API __attribute__((visibility("default")))
+#else
+#define ISLBM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum islbm_status {
+    ISLBM_OK = 0,
+    ISLBM_ERR_INVALID_ARGUMENT = 1,
+    ISLBM_ERR_CUDA = 2,
+    ISLBM_ERR_OUT_OF_MEMORY = 3,
+    ISLBM_ERR_HBM_BUDGET = 4,      /* the solve does not fit the handle's HBM budget */
+    ISLBM_ERR_NONFINITE = 5,       /* a NaN/Inf was found in the state */
+    ISLBM_ERR_NOT_SUPPORTED = 6,
+    ISLBM_ERR_NO_DEVICE = 7
+} islbm_status;
+
+typedef enum islbm_precision {
+    ISLBM_FP64 = 0,       /* distributions and arithmetic in FP64 (parity path) */
+    ISLBM_FP32 = 1,       /* distributions and arithmetic in FP32 */
+    ISLBM_FP16_DEV = 2,   /* distributions stored as FP16 deviations f_i - w_i, FP32 arithmetic */
+    ISLBM_BF16_DEV = 3    /* distributions stored as BF16 deviations f_i - w_i, FP32 arithmetic */
+} islbm_precision;
+
+typedef enum islbm_layout {
+    ISLBM_LAYOUT_UNIQUE = 0,     /* NZ x NY x NX unique nodes, x fastest: [z][y][x] */
+    ISLBM_LAYOUT_REFERENCE = 1   /* NYD6 x NZ6 x NX6 with ghosts, index j*NX6*NZ6 + k*NX6 + i
+                                    (C/initialization.h:20); periodic ghosts and the duplicated
+                                    end nodes are filled, the z ghost layers are zero */
+} islbm_layout;
+
+typedef enum islbm_kernel {
+    ISLBM_KERNEL_AUTO = 0,       /* tiled kernel when the grid allows it, else gather kernel */
+    ISLBM_KERNEL_GATHER = 1,     /* one thread per node, stencils read through L1/L2 */
+    ISLBM_KERNEL_TILED = 2       /* z-marching x-y tiles staged in shared memory */
+} islbm_kernel;
+
+/* Parameter set of C/variables.h (same names where the reference has one). */
+typedef struct islbm_params {
+    int NX, NY, NZ;            /* grid: spanwise, streamwise, wall-normal */
+    double LX, LY, LZ;         /* domain (4.5, 9.0, 3.036; hill height 1) */
+    double CFL;                /* minSize = (LZ-1)/NZ*CFL, dt = minSize */
+    double LXi;                /* computational extent of the xi coordinate (10.0) */
+    double Re;                 /* Reynolds number on hill height and Uref */
+    double Uref;               /* bulk velocity; tau = 0.5 + 3*Uref/(Re*minSize) */
+    int NDTFRC;                /* forcing-controller period in steps (C/variables.h:48) */
+    int precision;             /* islbm_precision */
+    double les_cs;             /* Smagorinsky constant (0 = plain MRT) */
+    double alpha;              /* hill steepness: footprint scaled by alpha (1 = reference) */
+    int init_mode;             /* 0: rest state of InitialUsingDftFunc; 1: v = Uref + noise */
+    unsigned long long seed;   /* noise seed for init_mode 1 */
+    double perturb;            /* noise amplitude relative to Uref (0.01 = +/-1 %) */
+    int mass_interval;         /* rho_modify every mass_interval steps (0 = off) */
+    int bfl_mode;              /* 0: BFL weight tables indexed as the reference does (x by i,
+                                  y by j, C/evolution.h:525-527); 1: by the wall row */
+    int device;                /* CUDA device ordinal */
+    int kernel;                /* islbm_kernel */
+    size_t hbm_budget_bytes;   /* refuse solves above this many device bytes (0 = no limit) */
+} islbm_params;
+
+typedef struct islbm_handle islbm_handle;
+
+/* Fill `p` with the reference's defaults (C/variables.h) and the 64x32x48 hill case. */
+ISLBM_API int islbm_default_params(islbm_params *p);
+
+/* Device bytes islbm_init would allocate for `p` (no device needed). */
+ISLBM_API int islbm_required_bytes(const islbm_params *p, size_t *bytes);
+
+/* Build mesh, weights and BFL tables in FP64 on the host, upload them, set the initial
+ * state and the initial body force (C/initialization.h:46). */
+ISLBM_API int islbm_init(const islbm_params *p, islbm_handle **out);
+
+/* Advance nsteps lattice steps (asynchronous on the handle's stream). The macroscopic
+ * fields of the last step are kept for islbm_fields. */
+ISLBM_API int islbm_step(islbm_handle *h, int nsteps);
+
+/* Copy rho, u, v, w of the last step to host buffers (FP64, `layout`); any pointer may be
+ * NULL. Before the first step these are the initial fields. Synchronises the stream. */
+ISLBM_API int islbm_fields(islbm_handle *h, double *rho, double *u, double *v, double *w, int layout);
+
+/* Copy population q (full value f_q, FP64) of the current state to a host buffer. */
+ISLBM_API int islbm_get_population(islbm_handle *h, int q, double *out, int layout);
+
+/* Replace the current state: f19 holds 19 consecutive arrays in `layout` (FP64). Restart
+ * path of InitialUsingBkpData (C/fileIO.h:315-354). */
+ISLBM_API int islbm_set_populations(islbm_handle *h, const double *f19, int layout);
+
+/* Controller state: body force (Force_d), mass correction (rho_modify_d), steps taken. */
+ISLBM_API int islbm_get_scalars(islbm_handle *h, double *force, double *rho_modify, long long *steps);
+ISLBM_API int islbm_set_force(islbm_handle *h, double force);
+
+/* Derived constants: tau, niu, Uref, minSize (C/variables.h:22, 76, 97-101). */
+ISLBM_API int islbm_get_constants(islbm_handle *h, double *tau, double *niu, double *uref, double *min_size);
+
+/* Device bytes of the weight tables as stored (per (y, z, direction)) and as they would be
+ * stored per node. */
+ISLBM_API int islbm_weight_table_bytes(islbm_handle *h, size_t *stored, size_t *per_node);
+
+/* The handle's CUDA stream (cudaStream_t) for event timing by the caller. */
+ISLBM_API int islbm_get_stream(islbm_handle *h, void **stream);
+
+/* Wait for all work on the handle's stream; returns ISLBM_ERR_CUDA on a device error. */
+ISLBM_API int islbm_sync(islbm_handle *h);
+
+/* Count non-finite values in the current state (0 = healthy). */
+ISLBM_API int islbm_check_finite(islbm_handle *h, long long *bad);
+
+ISLBM_API int islbm_destroy(islbm_handle *h);
+
+ISLBM_API const char *islbm_status_string(int status);
+
+/* Host-side precompute tables for a parameter set, no device needed (reference layout
+ * indexing, FP64). Names: "x","y","z","xi","XPara0","XPara2","YPara0","YPara2",
+ * "XiF3".."XiF18","Q3","Q4","Q15","Q16", BFL weight tables "XBFL37"... (idx = 0..6).
+ * Returns the element count in *count. */
+ISLBM_API int islbm_host_table(const islbm_params *p, const char *name, int idx, double *out, size_t cap, size_t *count);
+ISLBM_API int islbm_host_table_int(const islbm_params *p, const char *name, int *out, size_t cap, size_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
