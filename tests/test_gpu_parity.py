@@ -1,7 +1,7 @@
 """Parity of the CUDA step (through the C ABI) with the CPU oracle.
 
-Tolerances (relative L2 over the unique nodes):
-  FP64                 1e-12 on rho, u, v, w and the body force (the reference's own target)
+Tolerances (relative L2 over the unique nodes; "velocity" is the (u, v, w) vector field):
+  FP64                 1e-12 on rho, the velocity and the body force (the reference's target)
   FP32                 2e-5 on rho and the velocity after 100 steps
   FP16 / BF16 storage  deviation storage errors against the FP64 oracle: 1e-5 / 1e-4 on rho,
                        2e-2 / 1e-1 on the velocity after 100 steps
@@ -37,6 +37,14 @@ def velocity(d):
     return np.stack([d["u"], d["v"], d["w"]])
 
 
+def re_for_tau(tau, nz, ub=0.05):
+    """Reynolds number giving relaxation time tau on a grid with NZ wall-normal nodes.
+    The reference's step (and so the oracle) diverges for tau below about 0.56 on these
+    grids; long runs use tau = 0.6 (the reference's own default is tau = 0.6833)."""
+    min_size = (3.036 - 1.0) / nz * 0.6
+    return 3.0 * ub / ((tau - 0.5) * min_size)
+
+
 @pytest.mark.parametrize("kernel", [1, 0])
 @pytest.mark.parametrize("steps", [1, 25])
 def test_fp64_small_grid(islbm_lib, oracle_mod, kernel, steps):
@@ -60,38 +68,59 @@ def test_fp64_golden_fixture(islbm_lib):
 @pytest.mark.parametrize("opts", [dict(bfl_mode=1), dict(mass_interval=5), dict(les_cs=0.1),
                                   dict(init_mode=0), dict(alpha=1.3)])
 def test_fp64_options(islbm_lib, oracle_mod, opts):
-    steps = 30
-    g = solve(islbm_lib, steps, NX=8, NY=16, NZ=16, NDTFRC=10, precision="fp64", **opts)
-    r = oracle_run(oracle_mod, steps, 8, 16, 16, ndtfrc=10, **opts)
-    for n in ("rho", "u", "v", "w"):
-        assert rel_l2(g[n], r[n]) <= 1e-12, (n, opts)
+    steps = 60
+    re = re_for_tau(0.6, 16)
+    g = solve(islbm_lib, steps, NX=8, NY=16, NZ=16, NDTFRC=10, precision="fp64", Re=re, **opts)
+    r = oracle_run(oracle_mod, steps, 8, 16, 16, ndtfrc=10, re=re, **opts)
+    assert rel_l2(g["rho"], r["rho"]) <= 1e-12, opts
+    assert rel_l2(g["f"], r["f"]) <= 1e-12, opts
+    if opts.get("init_mode", 1) == 1:   # from rest the velocity is round-off only
+        assert rel_l2(velocity(g), velocity(r)) <= 1e-12, opts
     assert abs(g["force"] - r["force"]) <= 1e-12 * abs(r["force"])
 
 
 @pytest.mark.slow
 def test_fp64_hill64_1000_steps(islbm_lib, oracle_mod):
-    """The parity target: 64x32x48 (NY x NX x NZ), Re 700, 1000 steps, controller on."""
+    """The parity target: the 64x32x48 grid (NY x NX x NZ), 1000 steps, controller on, at
+    tau = 0.6 (Re_h = 59); at Re_h 700 the reference's step itself diverges (see
+    test_fp64_hill64_re700_before_divergence and tests/test_reference_stability.py)."""
     steps = 1000
-    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision="fp64")
-    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100)
+    re = re_for_tau(0.6, 48)
+    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision="fp64", Re=re)
+    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100, re=re)
+    assert np.isfinite(r["rho"]).all()
     assert rel_l2(g["rho"], r["rho"]) <= 1e-12
     assert rel_l2(velocity(g), velocity(r)) <= 1e-12
     assert abs(g["force"] - r["force"]) <= 1e-12 * abs(r["force"])
 
 
+def test_fp64_hill64_re700_before_divergence(islbm_lib, oracle_mod):
+    """The benchmark inputs (Re_h 700, perturbed start): parity while the reference's own
+    step is still finite (it leaves the representable range after about 60 steps)."""
+    steps = 15
+    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision="fp64", Re=700.0)
+    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100, re=700.0)
+    assert rel_l2(g["rho"], r["rho"]) <= 1e-12
+    assert rel_l2(velocity(g), velocity(r)) <= 1e-12
+
+
 def test_fp32_vs_oracle(islbm_lib, oracle_mod):
-    steps = 100
-    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision="fp32")
-    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100)
-    assert rel_l2(g["rho"], r["rho"]) <= 2e-5
-    assert rel_l2(velocity(g), velocity(r)) <= 2e-5
+    steps = 200
+    re = re_for_tau(0.6, 48)
+    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision="fp32", Re=re)
+    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100, re=re)
+    e_rho, e_u = rel_l2(g["rho"], r["rho"]), rel_l2(velocity(g), velocity(r))
+    print("fp32 rho", e_rho, "u", e_u)
+    assert e_rho <= 2e-5
+    assert e_u <= 2e-5
 
 
 @pytest.mark.parametrize("prec,tol_rho,tol_u", [("fp16", 1e-5, 2e-2), ("bf16", 1e-4, 1e-1)])
 def test_deviation_storage_vs_oracle(islbm_lib, oracle_mod, prec, tol_rho, tol_u):
-    steps = 100
-    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision=prec)
-    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100)
+    steps = 200
+    re = re_for_tau(0.6, 48)
+    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision=prec, Re=re)
+    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100, re=re)
     e_rho, e_u = rel_l2(g["rho"], r["rho"]), rel_l2(velocity(g), velocity(r))
     print(prec, "rho", e_rho, "u", e_u)
     assert e_rho <= tol_rho
@@ -118,6 +147,7 @@ def test_population_roundtrip_and_reference_layout(islbm_lib, oracle_mod):
 
 
 def test_rest_state_is_a_fixed_point(islbm_lib):
+    # rest state with zero body force: equilibrium everywhere, streaming of a uniform field
     p = islbm_lib.default_params(NX=8, NY=16, NZ=16, NDTFRC=10 ** 6, precision="fp64", init_mode=0)
     with islbm_lib.Solver(p) as s:
         s.force = 0.0

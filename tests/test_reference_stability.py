@@ -1,0 +1,27 @@
+"""Pins a property of the reference's step itself (through the oracle, which is bit-exact to
+the reference built for host cores): on the 64x32x48 hill grid it is stable at the
+reference's own relaxation time range (tau = 0.6) and diverges at Re_h = 700 (tau = 0.508),
+even from the rest state. The CUDA step reproduces this (tests/test_gpu_parity.py)."""
+import numpy as np
+
+
+def min_size(nz):
+    return (3.036 - 1.0) / nz * 0.6
+
+
+def test_stable_at_tau_0_6(oracle_mod):
+    re = 3 * 0.05 / (0.1 * min_size(48))
+    o = oracle_mod.Oracle(32, 64, 48, re=re, ndtfrc=100)
+    o.step(80)
+    rho = o.unique(o.get("rho"))
+    assert np.isfinite(rho).all() and rho.min() > 0.9 and rho.max() < 1.1
+
+
+def test_diverges_at_re_700_from_rest(oracle_mod):
+    o = oracle_mod.Oracle(32, 64, 48, re=700.0, init_mode=0, ndtfrc=100)
+    o.step(20)
+    early = np.abs(o.unique(o.get("rho")) - 1).max()
+    o.step(60)
+    late = np.abs(o.unique(o.get("rho")) - 1).max()
+    assert early < 1e-3
+    assert not (late < 1.0)   # grown by orders of magnitude (or non-finite)
