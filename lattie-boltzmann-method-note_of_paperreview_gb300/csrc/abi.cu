@@ -15,6 +15,7 @@
 #include "../../include/islbm.h"
 #include "geometry.hpp"
 #include "step_launch.hpp"
+#include "step_tiled.hpp"
 
 using namespace islbm;
 
@@ -37,6 +38,7 @@ struct islbm_handle {
     int cur = 0;
     unsigned long long steps = 0;
     bool use_tiled = false;
+    TiledConst tiled{};
 };
 
 namespace {
@@ -331,6 +333,16 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     h->use_tiled = false;
     if (p.kernel == ISLBM_KERNEL_TILED || p.kernel == ISLBM_KERNEL_AUTO) {
         h->use_tiled = tiled_supported(k, p.precision);
+        if (h->use_tiled) {
+            int sms = 0;
+            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+            double wx0[7], wx2[7], wy0[7], wy2[7];
+            for (int a = 0; a < 7; a++) {   // uniform spacing: the weights of the first node serve all
+                wx0[a] = h->g.XP0[(size_t)a*h->g.NX6 + 3]; wx2[a] = h->g.XP2[(size_t)a*h->g.NX6 + 3];
+                wy0[a] = h->g.YP0[(size_t)a*h->g.NYD6 + 3]; wy2[a] = h->g.YP2[(size_t)a*h->g.NYD6 + 3];
+            }
+            if (make_tiled_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) != 0) h->use_tiled = false;
+        }
         if (p.kernel == ISLBM_KERNEL_TILED && !h->use_tiled) { g_last = "tiled kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
     }
     CK(cudaDeviceSynchronize());
@@ -387,6 +399,7 @@ int islbm_step(islbm_handle *h, int nsteps) {
     L.ctrl = h->ctrl;
     L.les = h->p.les_cs > 0.0;
     L.stream = h->stream;
+    L.tiled = &h->tiled;
     for (int s = 0; s < nsteps; s++) {
         const unsigned long long n = h->steps + 1;
         L.fo = h->fbuf[h->cur];
@@ -490,6 +503,9 @@ int islbm_sync(islbm_handle *h) {
     if (check_handle(h)) return ISLBM_ERR_INVALID_ARGUMENT;
     CK(cudaSetDevice(h->device));
     CK(cudaStreamSynchronize(h->stream));
+    unsigned fault = 0;
+    CK(cudaMemcpy(&fault, &h->ctrl->fault, sizeof(fault), cudaMemcpyDeviceToHost));
+    if (fault) { g_last = "a shared-memory pipeline wait timed out in the step kernel"; return ISLBM_ERR_CUDA; }
     return ISLBM_OK;
 }
 

@@ -65,6 +65,7 @@ struct Ctrl {
     unsigned long long step; // completed steps
     unsigned int done;       // blocks finished in the running step
     unsigned int nonfinite;  // set when a non-finite density is produced
+    unsigned int fault;      // set when a pipeline wait gave up (bounded waits)
 };
 
 template <class C> struct Tables {

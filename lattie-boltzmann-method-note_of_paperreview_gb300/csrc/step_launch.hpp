@@ -18,6 +18,7 @@ struct StepLaunch {
     unsigned long long n;      // 1-based number of the step being computed
     bool les, macros_on, mass;
     void *macros[4];           // rho, u, v, w (compute type) when macros_on
+    const void *tiled;         // TiledConst for the tiled kernel
     cudaStream_t stream;
 };
 

@@ -1,0 +1,25 @@
+// Launch constants of the tiled step kernel (host-computed, passed by value).
+#pragma once
+
+#include <stddef.h>
+
+#include "step_common.cuh"
+
+namespace islbm {
+
+struct TiledConst {
+    int TY;                       // streamwise rows per tile (256 / NX)
+    int grid;                     // persistent CTAs
+    long long units;              // tiles * NZ (flattened work)
+    int off[19];                  // element offset of each population's region within a stage
+    int rows[19];                 // rows staged per population (TY, or TY + 6 with the halo)
+    size_t stage_elems, stage_bytes, smem_bytes;
+    unsigned stage_bytes_used;    // bytes the bulk copies of one plane deliver
+    float wx0[7], wx2[7], wy0[7], wy2[7];   // uniform-spacing Lagrange weights
+    unsigned long long n;         // step number (set per launch)
+};
+
+int make_tiled_const(const StepConst &k, int precision, const double *wx0, const double *wx2, const double *wy0,
+                     const double *wy2, int num_sms, TiledConst *out);
+
+}  // namespace islbm

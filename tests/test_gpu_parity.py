@@ -167,3 +167,29 @@ def test_nonfinite_state_is_reported(islbm_lib):
         s.set_populations(f)
         s.step(1)
         assert not s.healthy()
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp16", 2e-3), ("bf16", 1e-2)])
+@pytest.mark.parametrize("les", [0.0, 0.1])
+def test_tiled_matches_gather(islbm_lib, prec, tol, les):
+    """The shared-memory tiled kernel against the gather kernel on the 64x32x48 grid (same
+    storage format; they differ only in FP32 summation order)."""
+    steps = 40
+    re = re_for_tau(0.6, 48)
+    kw = dict(NX=32, NY=64, NZ=48, NDTFRC=10, precision=prec, Re=re, les_cs=les, mass_interval=7)
+    a = solve(islbm_lib, steps, kernel=1, **kw)
+    b = solve(islbm_lib, steps, kernel=2, **kw)
+    assert rel_l2(b["rho"], a["rho"]) <= tol
+    assert rel_l2(velocity(b), velocity(a)) <= 50 * tol
+    assert abs(b["force"] - a["force"]) <= 1e-3 * abs(a["force"])
+
+
+def test_tiled_wide_grid_vs_oracle(islbm_lib, oracle_mod):
+    """A 128-wide spanwise grid (two streamwise rows per tile) and a bfl_mode-1 run."""
+    steps = 30
+    nz = 24
+    re = re_for_tau(0.6, nz)
+    g = solve(islbm_lib, steps, NX=128, NY=32, NZ=nz, NDTFRC=10, precision="fp32", Re=re, kernel=2, bfl_mode=1)
+    r = oracle_run(oracle_mod, steps, 128, 32, nz, ndtfrc=10, re=re, bfl_mode=1)
+    assert rel_l2(g["rho"], r["rho"]) <= 1e-5
+    assert rel_l2(velocity(g), velocity(r)) <= 1e-4
