@@ -29,7 +29,7 @@ namespace islbm {
 namespace {
 
 constexpr int NTHREADS = 256;
-constexpr int NSTAGES = 3;
+constexpr int NSTAGES = 4;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -171,6 +171,8 @@ struct Ring {
 
 template <class S, bool LES>
 struct TiledKernel {
+    // per-launch float constants (computed once per thread from the FP64 controller state)
+    struct Scal { float f6, f12, rho_mod, tau, lesC; };
     const S *__restrict__ fo;
     S *__restrict__ fn;
     Tables<float> T;
@@ -180,38 +182,64 @@ struct TiledKernel {
     float *rho_out, *u_out, *v_out, *w_out;
     int macros_on, mass_on;
 
-    // one target node: xi combination, walls, BFL, collision, store
+    // one target node: xi combination, walls, BFL, collision, store. `wv` points at the 64 xi
+    // weights of (y, z) (shared memory for interior targets, global for the wall caps).
     template <int SLOT12>
-    __device__ __forceinline__ void target(const Ring &R, int x, int y, int z, double &ub, double &mass) const {
+    __device__ __forceinline__ void target(const Ring &R, int x, int y, int z, const float *wv_, float f0, const Scal &sc,
+                                           double &ub, double &mass) const {
         const int NX = k.NX, NY = k.NY;
         const size_t N = (size_t)NX*NY*k.NZ;
         const size_t node = ((size_t)z*NY + y)*NX + x;
-        const float4 *wv = (const float4 *)(T.wxi + ((size_t)z*NY + y)*64);
-        float xi[8][7];
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            const float4 a = __ldg(wv + 2*t), b = __ldg(wv + 2*t + 1);
-            xi[t][0] = a.x; xi[t][1] = a.y; xi[t][2] = a.z; xi[t][3] = a.w; xi[t][4] = b.x; xi[t][5] = b.y; xi[t][6] = b.z;
-        }
+        const float4 *wv = (const float4 *)wv_;
         float F[19];
-        F[0] = load_f<S>(fo, node, 0);
+        F[0] = f0;
         F[1] = R.r12[SLOT12].x; F[2] = R.r12[SLOT12].y;
-        float s[16];
+        // xi combination, one weight table at a time (8 live weights instead of 56)
+        auto table = [&](int t, float (&w)[7]) {
+            const float4 a = wv[2*t], b = wv[2*t + 1];
+            w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z;
+        };
+        {
+            float w[7];
+            table(XI3, w);
+            float f3 = 0, f7 = 0, f8 = 0;
 #pragma unroll
-        for (int i = 0; i < 16; i++) s[i] = 0.f;
+            for (int c = 0; c < 7; c++) { f3 += w[c]*R.r34[c].x; f7 += w[c]*R.r78[c].x; f8 += w[c]*R.r78[c].y; }
+            F[3] = f3; F[7] = f7; F[8] = f8;
+            table(XI4, w);
+            float f4 = 0, f9 = 0, f10 = 0;
 #pragma unroll
-        for (int c = 0; c < 7; c++) {
-            s[0] += xi[XI3][c]*R.r34[c].x;   s[1] += xi[XI4][c]*R.r34[c].y;
-            s[2] += xi[XI5][c]*R.r56[c].x;   s[3] += xi[XI6][c]*R.r56[c].y;
-            s[4] += xi[XI3][c]*R.r78[c].x;   s[5] += xi[XI3][c]*R.r78[c].y;
-            s[6] += xi[XI4][c]*R.r910[c].x;  s[7] += xi[XI4][c]*R.r910[c].y;
-            s[8] += xi[XI5][c]*R.r1112[c].x; s[9] += xi[XI5][c]*R.r1112[c].y;
-            s[10] += xi[XI6][c]*R.r1314[c].x; s[11] += xi[XI6][c]*R.r1314[c].y;
-            s[12] += xi[XI15][c]*R.r1516[c].x; s[13] += xi[XI16][c]*R.r1516[c].y;
-            s[14] += xi[XI17][c]*R.r1718[c].x; s[15] += xi[XI18][c]*R.r1718[c].y;
+            for (int c = 0; c < 7; c++) { f4 += w[c]*R.r34[c].y; f9 += w[c]*R.r910[c].x; f10 += w[c]*R.r910[c].y; }
+            F[4] = f4; F[9] = f9; F[10] = f10;
+            table(XI5, w);
+            float f5 = 0, f11 = 0, f12 = 0;
+#pragma unroll
+            for (int c = 0; c < 7; c++) { f5 += w[c]*R.r56[c].x; f11 += w[c]*R.r1112[c].x; f12 += w[c]*R.r1112[c].y; }
+            F[5] = f5; F[11] = f11; F[12] = f12;
+            table(XI6, w);
+            float f6 = 0, f13 = 0, f14 = 0;
+#pragma unroll
+            for (int c = 0; c < 7; c++) { f6 += w[c]*R.r56[c].y; f13 += w[c]*R.r1314[c].x; f14 += w[c]*R.r1314[c].y; }
+            F[6] = f6; F[13] = f13; F[14] = f14;
+            float g = 0;
+            table(XI15, w);
+#pragma unroll
+            for (int c = 0; c < 7; c++) g += w[c]*R.r1516[c].x;
+            F[15] = g; g = 0;
+            table(XI16, w);
+#pragma unroll
+            for (int c = 0; c < 7; c++) g += w[c]*R.r1516[c].y;
+            F[16] = g; g = 0;
+            table(XI17, w);
+#pragma unroll
+            for (int c = 0; c < 7; c++) g += w[c]*R.r1718[c].x;
+            F[17] = g; g = 0;
+            table(XI18, w);
+#pragma unroll
+            for (int c = 0; c < 7; c++) g += w[c]*R.r1718[c].y;
+            F[18] = g;
         }
-#pragma unroll
-        for (int q = 3; q < 19; q++) F[q] = s[q - 3];
+
         if (z == 0) {
             const S *b = fo + node;
             F[5] = load_f<S>(b + 6*N, 0, 6); F[11] = load_f<S>(b + 14*N, 0, 14); F[12] = load_f<S>(b + 13*N, 0, 13);
@@ -226,50 +254,161 @@ struct TiledKernel {
             const int nb = 2*k.NYD6, r = z*k.NYD6 + (y + 3);
             if (T.bfl_flag[r] | T.bfl_flag[nb + r] | T.bfl_flag[2*nb + r] | T.bfl_flag[3*nb + r]) bfl_node<S>(fo, T, k, x, y, z, F);
         }
-        const double force = ctrl->force;
-        const float f6 = (float)(1.0/6*force*k.dt), f12 = (float)(1.0/12*force*k.dt);
         float rho_s, u1, v1, w1;
-        collide_node<float, LES>(F, (float)ctrl->rho_modify, f6, f12, (float)k.tau, (float)k.les_C, rho_s, u1, v1, w1);
+        collide_node<float, LES>(F, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
 #pragma unroll
         for (int q = 0; q < 19; q++) store_f<S>(fn + (size_t)q*N, node, q, F[q]);
         if (macros_on) { rho_out[node] = rho_s; u_out[node] = u1; v_out[node] = v1; w_out[node] = w1; }
         if (y == k.yplane) ub += (double)v1*T.dxv[x]*T.dzv[z];
-        if (mass_on) mass += (double)rho_s;
+        if (mass_on) mass += rho_s;
         if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
     }
 
-    __device__ void issue_plane(S *stage, uint64_t *bar, int p, int y0) const {
-        const int NX = k.NX, NY = k.NY, TY = tc.TY;
-        const size_t N = (size_t)NX*NY*k.NZ;
+    // Copies of plane p into one stage: the 18 moving populations (with the streamwise halo
+    // where needed) and, when plane p completes the window of an interior target z = p - 3,
+    // that target's xi weights and f0 row.
+    // Issued by warp 0: lane 0 posts the expected bytes, then lane q copies population q
+    // (two pieces when the halo wraps) and lanes 19, 20 the target data.
+    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, int lane) const {
+        const int NX = k.NX, NY = k.NY, NZ = k.NZ, TY = tc.TY;
+        const size_t N = (size_t)NX*NY*NZ;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
-        mbar_expect_tx(bar, tc.stage_bytes_used);
-        for (int q = 1; q < 19; q++) {
-            S *dst = stage + tc.off[q];
+        const bool tgt = p >= 7 && p <= NZ - 1;
+        if (lane == 0) mbar_expect_tx(bar, tc.stage_bytes_used + (tgt ? tc.tgt_bytes : 0u));
+        __syncwarp();
+        S *pops = (S *)stage;
+        const int q = lane;
+        if (q >= 1 && q < 19) {
+            S *dst = pops + tc.off[q];
             const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
             if (tc.rows[q] == TY) {
                 bulk_g2s(dst, plane_base + (size_t)y0*NX, TY*row_bytes, bar);
             } else {
-                const int ys = wrapi(y0 - 3, NY);
+                const int ys = y0 >= 3 ? y0 - 3 : y0 - 3 + NY;
                 const int rows = TY + 6;
                 const int first = min(rows, NY - ys);
                 bulk_g2s(dst, plane_base + (size_t)ys*NX, first*row_bytes, bar);
                 if (first < rows) bulk_g2s(dst + (size_t)first*NX, plane_base, (rows - first)*row_bytes, bar);
             }
         }
+        if (tgt && lane == 19) {
+            const int z = p - 3;
+            bulk_g2s(stage + tc.w_off, T.wxi + ((size_t)z*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
+        }
+        if (tgt && lane == 20) {
+            const int z = p - 3;
+            bulk_g2s(stage + tc.f0_off, fo + ((size_t)z*NY + y0)*NX, TY*row_bytes, bar);
+        }
+    }
+
+    struct Lane {
+        int tid, xl, yl;        // node of this thread within the tile
+        int xr, xx0;            // spanwise-filter task: row and first of two nodes
+        int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
+    };
+
+    // One source plane: wait for its copies, advance the ring, filter, store into ring slot 6.
+    __device__ __forceinline__ void plane(int i, int p, int p1, int y0, unsigned char *smem, Ring &R, unsigned &parity,
+                                          bool &faulted, const Lane &L) const {
+        const int NX = k.NX, TY = tc.TY;
+        const int s = i % NSTAGES;
+        uint64_t *bars = (uint64_t *)(smem + tc.bar_off);
+        float *ybuf = (float *)(smem + tc.ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
+        float *xbuf = (float *)(smem + tc.xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
+        unsigned char *stage = smem + (size_t)s*tc.stage_bytes;
+        const S *raw = (const S *)stage;
+        mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted);
+        parity ^= 1u << s;
+        R.shift();
+        {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
+            auto row = [&](int q, int lr) -> const S * { return raw + tc.off[q] + lr*NX + L.xl; };
+            float a3 = 0, a4 = 0, a15 = 0, a16 = 0, a17 = 0, a18 = 0, a7 = 0, a8 = 0, a9 = 0, a10 = 0;
+#pragma unroll
+            for (int b = 0; b < 7; b++) {
+                const float y0w = tc.wy0[b], y2w = tc.wy2[b];
+                const int lr = L.yl + b;
+                a3 += y0w*ld1<S>(row(3, lr), 1.f/18); a4 += y2w*ld1<S>(row(4, lr), 1.f/18);
+                a15 += y0w*ld1<S>(row(15, lr), 1.f/36); a16 += y2w*ld1<S>(row(16, lr), 1.f/36);
+                a17 += y0w*ld1<S>(row(17, lr), 1.f/36); a18 += y2w*ld1<S>(row(18, lr), 1.f/36);
+                a7 += y0w*ld1<S>(row(7, lr), 1.f/36); a8 += y0w*ld1<S>(row(8, lr), 1.f/36);
+                a9 += y2w*ld1<S>(row(9, lr), 1.f/36); a10 += y2w*ld1<S>(row(10, lr), 1.f/36);
+            }
+            R.r34[6] = make_float2(a3, a4);
+            R.r1516[6] = make_float2(a15, a16);
+            R.r1718[6] = make_float2(a17, a18);
+            R.r56[6] = make_float2(ld1<S>(row(5, L.yl), 1.f/18), ld1<S>(row(6, L.yl), 1.f/18));
+            const int o = L.yl*NX + L.xl;
+            ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
+        }
+        __syncthreads();
+        // every thread has finished plane i-1: its stage can take plane i + NSTAGES - 1
+        if (L.tid < 32 && p + NSTAGES - 1 <= p1) {
+            fence_proxy_async();
+            const int sn = (i + NSTAGES - 1) % NSTAGES;
+            issue_plane(smem + (size_t)sn*tc.stage_bytes, &bars[sn], p + NSTAGES - 1, y0, L.tid);
+        }
+        {   // spanwise filter: two nodes of one row, five directions of one departure side
+            const int m = NX - 1;
+            const int x0 = L.xx0;
+            const int xa = (x0 - 4) & m, xb = (x0 - 2) & m, xc = x0, xd = (x0 + 2) & m, xe = (x0 + 4) & m;
+#pragma unroll
+            for (int j = 0; j < 5; j++) {
+                const int d = 2*j + L.xsel;        // xbuf slot: 7, 8, 9, 10, 1, 2, 11, 12, 13, 14
+                float v[10];
+                if (j < 2) {
+                    const float *in = ybuf + (size_t)d*TY*NX + L.xr*NX;
+                    const float2 a = *(const float2 *)(in + xa), b = *(const float2 *)(in + xb), c = *(const float2 *)(in + xc),
+                                 e = *(const float2 *)(in + xd), g = *(const float2 *)(in + xe);
+                    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = e.x; v[7] = e.y; v[8] = g.x; v[9] = g.y;
+                } else {
+                    const int q = d == 4 ? 1 : (d == 5 ? 2 : d + 5);
+                    const float w = q <= 2 ? 1.f/18 : 1.f/36;
+                    const S *in = raw + tc.off[q] + L.xr*NX;
+                    v[0] = ld1<S>(in + xa, w); v[1] = ld1<S>(in + xa + 1, w); v[2] = ld1<S>(in + xb, w); v[3] = ld1<S>(in + xb + 1, w);
+                    v[4] = ld1<S>(in + xc, w); v[5] = ld1<S>(in + xc + 1, w); v[6] = ld1<S>(in + xd, w); v[7] = ld1<S>(in + xd + 1, w);
+                    v[8] = ld1<S>(in + xe, w); v[9] = ld1<S>(in + xe + 1, w);
+                }
+                float o0 = 0, o1 = 0;
+#pragma unroll
+                for (int a = 0; a < 7; a++) {
+                    const float w = L.xsel ? tc.wx2[a] : tc.wx0[a];
+                    o0 += w*v[a + 1]; o1 += w*v[a + 2];
+                }
+                *(float2 *)(xbuf + (size_t)d*TY*NX + L.xr*NX + x0) = make_float2(o0, o1);
+            }
+        }
+        __syncthreads();
+        {
+            const int o = L.yl*NX + L.xl, st = TY*NX;
+            R.r78[6] = make_float2(xbuf[0*st + o], xbuf[1*st + o]);
+            R.r910[6] = make_float2(xbuf[2*st + o], xbuf[3*st + o]);
+            R.r12[6] = make_float2(xbuf[4*st + o], xbuf[5*st + o]);
+            R.r1112[6] = make_float2(xbuf[6*st + o], xbuf[7*st + o]);
+            R.r1314[6] = make_float2(xbuf[8*st + o], xbuf[9*st + o]);
+        }
+    }
+
+    template <int SLOT12>
+    __device__ __forceinline__ void cap_target(const Ring &R, int x, int y, int z, const Scal &sc, double &ub,
+                                               double &mass) const {
+        const size_t node = ((size_t)z*k.NY + y)*k.NX + x;
+        target<SLOT12>(R, x, y, z, T.wxi + ((size_t)z*k.NY + y)*64, load_f<S>(fo, node, 0), sc, ub, mass);
     }
 
     __device__ void run() const {
         extern __shared__ __align__(128) unsigned char smem[];
         const int NX = k.NX, NZ = k.NZ, TY = tc.TY;
-        S *stages = (S *)smem;
-        float *ybuf = (float *)(smem + NSTAGES*tc.stage_bytes);      // [4][TY][NX]  dirs 7, 8, 9, 10
-        float *xbuf = ybuf + 4*TY*NX;                                  // [10][TY][NX] dirs 7..10, 1, 2, 11..14
-        uint64_t *bars = (uint64_t *)(xbuf + 10*TY*NX);
-        const int tid = threadIdx.x;
-        const int xl = tid % NX, yl = tid / NX;
-        const int nxv4 = NX/4;
+        uint64_t *bars = (uint64_t *)(smem + tc.bar_off);
+        Lane L;
+        L.tid = threadIdx.x;
+        L.xl = L.tid & (NX - 1);
+        L.yl = L.tid >> tc.log2nx;
+        L.xsel = L.tid >> 7;                           // 128 threads per departure side
+        const int pair = L.tid & 127;                  // TY*NX/2 = 128 node pairs per plane
+        L.xr = pair >> (tc.log2nx - 1);
+        L.xx0 = 2*(pair & (NX/2 - 1));
 
-        if (tid == 0) {
+        if (L.tid == 0) {
             for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
             fence_mbar_init();
         }
@@ -278,120 +417,71 @@ struct TiledKernel {
         bool faulted = false;
 
         double ub = 0.0, mass = 0.0;
+        Scal sc;
+        {
+            const double force = ctrl->force;
+            sc.f6 = (float)(1.0/6*force*k.dt);
+            sc.f12 = (float)(1.0/12*force*k.dt);
+            sc.rho_mod = (float)ctrl->rho_modify;
+            sc.tau = (float)k.tau;
+            sc.lesC = (float)k.les_C;
+        }
         Ring R;
 #pragma unroll
         for (int s = 0; s < 7; s++) {
             R.r12[s] = R.r34[s] = R.r56[s] = R.r78[s] = R.r910[s] = make_float2(0.f, 0.f);
             R.r1112[s] = R.r1314[s] = R.r1516[s] = R.r1718[s] = make_float2(0.f, 0.f);
         }
-        const long long units = tc.units;
-        long long u0 = (long long)blockIdx.x*units/gridDim.x;
-        const long long u1 = (long long)(blockIdx.x + 1)*units/gridDim.x;
-        while (u0 < u1) {
-            const int tile = (int)(u0/NZ);
-            const int za = (int)(u0 - (long long)tile*NZ);
-            const int zb = (int)(min(u1, (long long)(tile + 1)*NZ) - (long long)tile*NZ);
-            u0 = (long long)tile*NZ + zb;
+        // whole columns: CTA b takes tiles b, b + G, b + 2G, ... so that the CTAs running at the
+        // same time hold neighbouring tiles at similar heights and share the halo rows in L2
+        const int ntiles = k.NY/TY;
+        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+            const int za = 0, zb = NZ;
             const int y0 = tile*TY;
             const int zl = zb - 1;
             const int p0 = za <= 3 ? 0 : (za >= NZ - 3 ? NZ - 7 : za - 3);
             const int p1 = zl <= 3 ? 6 : (zl >= NZ - 4 ? NZ - 1 : zl + 3);
-            const int nplanes = p1 - p0 + 1;
-            __syncthreads();   // previous segment done with every stage
-            if (tid == 0) {
+            __syncthreads();   // every thread is done with every stage of the previous segment
+            if (L.tid < 32) {
                 fence_proxy_async();
-                for (int s = 0; s < NSTAGES && s < nplanes; s++)
-                    issue_plane(stages + (size_t)s*tc.stage_elems, &bars[s], p0 + s, y0);
+                for (int s = 0; s < NSTAGES - 1 && p0 + s <= p1; s++)
+                    issue_plane(smem + (size_t)s*tc.stage_bytes, &bars[s], p0 + s, y0, L.tid);
             }
-            const int y = y0 + yl;
-            for (int i = 0; i < nplanes; i++) {
-                const int p = p0 + i;
-                const int s = i % NSTAGES;
-                mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted);
-                parity ^= 1u << s;
-                const S *raw = stages + (size_t)s*tc.stage_elems;
-                R.shift();
-                // streamwise filter (rows yl .. yl+6 of the halo copy) and raw values
-                {
-                    auto row = [&](int q, int lr) -> const S * { return raw + tc.off[q] + lr*NX + xl; };
-                    float a3 = 0, a4 = 0, a15 = 0, a16 = 0, a17 = 0, a18 = 0, a7 = 0, a8 = 0, a9 = 0, a10 = 0;
-#pragma unroll
-                    for (int b = 0; b < 7; b++) {
-                        const float y0w = tc.wy0[b], y2w = tc.wy2[b];
-                        a3 += y0w*ld1<S>(row(3, yl + b), 1.f/18); a4 += y2w*ld1<S>(row(4, yl + b), 1.f/18);
-                        a15 += y0w*ld1<S>(row(15, yl + b), 1.f/36); a16 += y2w*ld1<S>(row(16, yl + b), 1.f/36);
-                        a17 += y0w*ld1<S>(row(17, yl + b), 1.f/36); a18 += y2w*ld1<S>(row(18, yl + b), 1.f/36);
-                        a7 += y0w*ld1<S>(row(7, yl + b), 1.f/36); a8 += y0w*ld1<S>(row(8, yl + b), 1.f/36);
-                        a9 += y2w*ld1<S>(row(9, yl + b), 1.f/36); a10 += y2w*ld1<S>(row(10, yl + b), 1.f/36);
-                    }
-                    R.r34[6] = make_float2(a3, a4);
-                    R.r1516[6] = make_float2(a15, a16);
-                    R.r1718[6] = make_float2(a17, a18);
-                    R.r56[6] = make_float2(ld1<S>(row(5, yl), 1.f/18), ld1<S>(row(6, yl), 1.f/18));
-                    const int o = yl*NX + xl;
-                    ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
+            const int y = y0 + L.yl;
+            int i = 0, p = p0;
+            // warm-up: the six planes below the first window end
+#pragma unroll 1
+            for (; i < 6; i++, p++) plane(i, p, p1, y0, smem, R, parity, faulted, L);
+            if (p == 6) {   // window of the lower wall cap (targets 0..3 share planes 0..6)
+                plane(i, p, p1, y0, smem, R, parity, faulted, L);
+                if (za <= 0 && 0 < zb) cap_target<0>(R, L.xl, y, 0, sc, ub, mass);
+                if (za <= 1 && 1 < zb) cap_target<1>(R, L.xl, y, 1, sc, ub, mass);
+                if (za <= 2 && 2 < zb) cap_target<2>(R, L.xl, y, 2, sc, ub, mass);
+                if (za <= 3 && 3 < zb) cap_target<3>(R, L.xl, y, 3, sc, ub, mass);
+                i++; p++;
+            }
+            // steady state: each plane completes the window of one interior target
+            const int pend = min(p1, NZ - 2);
+#pragma unroll 1
+            for (; p <= pend; i++, p++) {
+                plane(i, p, p1, y0, smem, R, parity, faulted, L);
+                const unsigned char *stage = smem + (size_t)(i % NSTAGES)*tc.stage_bytes;
+                const float *wv = (const float *)(stage + tc.w_off) + L.yl*64;
+                const float f0 = ld1<S>((const S *)(stage + tc.f0_off) + L.yl*NX + L.xl, 1.f/3);
+                target<3>(R, L.xl, y, p - 3, wv, f0, sc, ub, mass);
+            }
+            if (p == NZ - 1 && p <= p1) {   // window of the upper wall cap
+                plane(i, p, p1, y0, smem, R, parity, faulted, L);
+                const int zt = NZ - 4;
+                if (za <= zt && zt < zb) {
+                    const unsigned char *stage = smem + (size_t)(i % NSTAGES)*tc.stage_bytes;
+                    const float *wv = (const float *)(stage + tc.w_off) + L.yl*64;
+                    const float f0 = ld1<S>((const S *)(stage + tc.f0_off) + L.yl*NX + L.xl, 1.f/3);
+                    target<3>(R, L.xl, y, zt, wv, f0, sc, ub, mass);
                 }
-                __syncthreads();
-                // spanwise filter, 4 nodes per task: dirs 7..10 from ybuf, 1, 2, 11..14 from the plane
-                for (int t = tid; t < 10*TY*nxv4; t += NTHREADS) {
-                    const int d = t/(TY*nxv4);
-                    const int rem = t - d*TY*nxv4;
-                    const int r = rem/nxv4, xb = rem - r*nxv4;
-                    const int x0 = xb*4;
-                    const int xm = wrapi(x0 - 4, NX), xp = wrapi(x0 + 4, NX);
-                    float v[12];
-                    if (d < 4) {
-                        const float *in = ybuf + (size_t)d*TY*NX + r*NX;
-                        const float4 a = ld4(in + xm), b = ld4(in + x0), c = ld4(in + xp);
-                        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-                        v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
-                    } else {
-                        const int q = d == 4 ? 1 : (d == 5 ? 2 : d + 5);   // 1, 2, 11, 12, 13, 14
-                        const float w = q <= 2 ? 1.f/18 : 1.f/36;
-                        const S *in = raw + tc.off[q] + r*NX;
-                        const float4 a = ld4<S>(in + xm, w), b = ld4<S>(in + x0, w), c = ld4<S>(in + xp, w);
-                        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-                        v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
-                    }
-                    // weights: departure x - minSize for 7, 9, 1, 11, 13; x + minSize for 8, 10, 2, 12, 14
-                    const bool minus = (d & 1) == 0;
-                    float o0 = 0, o1 = 0, o2 = 0, o3 = 0;
-#pragma unroll
-                    for (int a = 0; a < 7; a++) {
-                        const float w = minus ? tc.wx0[a] : tc.wx2[a];
-                        o0 += w*v[a + 1]; o1 += w*v[a + 2]; o2 += w*v[a + 3]; o3 += w*v[a + 4];
-                    }
-                    *(float4 *)(xbuf + (size_t)d*TY*NX + r*NX + x0) = make_float4(o0, o1, o2, o3);
-                }
-                __syncthreads();
-                if (tid == 0 && i + NSTAGES < nplanes) {
-                    fence_proxy_async();
-                    issue_plane(stages + (size_t)s*tc.stage_elems, &bars[s], p + NSTAGES, y0);
-                }
-                {
-                    const int o = yl*NX + xl, st = TY*NX;
-                    R.r78[6] = make_float2(xbuf[0*st + o], xbuf[1*st + o]);
-                    R.r910[6] = make_float2(xbuf[2*st + o], xbuf[3*st + o]);
-                    R.r12[6] = make_float2(xbuf[4*st + o], xbuf[5*st + o]);
-                    R.r1112[6] = make_float2(xbuf[6*st + o], xbuf[7*st + o]);
-                    R.r1314[6] = make_float2(xbuf[8*st + o], xbuf[9*st + o]);
-                }
-                // targets whose 7-plane window ends at plane p
-                if (p == 6) {
-                    if (za <= 0 && 0 < zb) target<0>(R, xl, y, 0, ub, mass);
-                    if (za <= 1 && 1 < zb) target<1>(R, xl, y, 1, ub, mass);
-                    if (za <= 2 && 2 < zb) target<2>(R, xl, y, 2, ub, mass);
-                    if (za <= 3 && 3 < zb) target<3>(R, xl, y, 3, ub, mass);
-                }
-                if (p >= 7) {
-                    const int zt = p - 3;
-                    if (zt <= NZ - 4 && za <= zt && zt < zb) target<3>(R, xl, y, zt, ub, mass);
-                }
-                if (p == NZ - 1) {
-                    if (za <= NZ - 3 && NZ - 3 < zb) target<4>(R, xl, y, NZ - 3, ub, mass);
-                    if (za <= NZ - 2 && NZ - 2 < zb) target<5>(R, xl, y, NZ - 2, ub, mass);
-                    if (za <= NZ - 1 && NZ - 1 < zb) target<6>(R, xl, y, NZ - 1, ub, mass);
-                }
+                if (za <= NZ - 3 && NZ - 3 < zb) cap_target<4>(R, L.xl, y, NZ - 3, sc, ub, mass);
+                if (za <= NZ - 2 && NZ - 2 < zb) cap_target<5>(R, L.xl, y, NZ - 2, sc, ub, mass);
+                if (za <= NZ - 1 && NZ - 1 < zb) cap_target<6>(R, L.xl, y, NZ - 1, sc, ub, mass);
             }
         }
         end_of_step<NTHREADS>(ctrl, k, tc.n, ub, mass, true, mass_on != 0);
@@ -436,7 +526,8 @@ size_t elem_bytes(int precision) { return precision == ISLBM_FP32 ? 4 : 2; }
 
 bool tiled_supported(const StepConst &k, int precision) {
     if (precision == ISLBM_FP64) return false;
-    if (k.NX < 8 || k.NX > NTHREADS || NTHREADS % k.NX != 0 || k.NX % 8 != 0) return false;
+    // NX a power of two in [8, 256] so that a tile is 256 nodes and index math is shifts
+    if (k.NX < 8 || k.NX > NTHREADS || (k.NX & (k.NX - 1)) != 0) return false;
     const int TY = NTHREADS/k.NX;
     if (k.NY % TY != 0 || k.NY < TY + 6 || k.NZ < 8) return false;
     return true;
@@ -447,33 +538,39 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     TiledConst tc;
     std::memset(&tc, 0, sizeof(tc));
     tc.TY = NTHREADS/k.NX;
+    int l = 0;
+    while ((1 << l) < k.NX) l++;
+    tc.log2nx = l;
     const size_t eb = elem_bytes(precision);
-    size_t off = 0;
+    auto up16 = [](size_t v) { return (v + 15)/16*16; };
+    size_t off = 0;   // bytes within a stage
     tc.off[0] = 0; tc.rows[0] = 0;
+    size_t used = 0;
     for (int q = 1; q < 19; q++) {
         const bool wide = (q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15);
         tc.rows[q] = wide ? tc.TY + 6 : tc.TY;
-        tc.off[q] = (int)off;
-        off += (size_t)tc.rows[q]*k.NX;
-        off = (off*eb + 15)/16*16/eb;   // keep every region 16-byte aligned
+        tc.off[q] = (int)(off/eb);
+        off = up16(off + (size_t)tc.rows[q]*k.NX*eb);
+        used += (size_t)tc.rows[q]*k.NX*eb;
     }
-    tc.stage_elems = off;
-    tc.stage_bytes = (off*eb + 127)/128*128;
-    tc.stage_elems = tc.stage_bytes/eb;
-    size_t used = 0;
-    for (int q = 1; q < 19; q++) used += (size_t)tc.rows[q]*k.NX*eb;
     tc.stage_bytes_used = (unsigned)used;
-    tc.smem_bytes = NSTAGES*tc.stage_bytes + (size_t)14*tc.TY*k.NX*sizeof(float) + NSTAGES*sizeof(uint64_t);
+    tc.w_off = (unsigned)off;
+    off = up16(off + (size_t)tc.TY*64*sizeof(float));
+    tc.f0_off = (unsigned)off;
+    off = up16(off + (size_t)tc.TY*k.NX*eb);
+    tc.tgt_bytes = (unsigned)(tc.TY*64*sizeof(float) + tc.TY*k.NX*eb);
+    tc.stage_bytes = (off + 127)/128*128;
+    tc.ybuf_off = NSTAGES*tc.stage_bytes;
+    tc.xbuf_off = tc.ybuf_off + (size_t)4*tc.TY*k.NX*sizeof(float);
+    tc.bar_off = tc.xbuf_off + (size_t)10*tc.TY*k.NX*sizeof(float);
+    tc.smem_bytes = tc.bar_off + NSTAGES*sizeof(uint64_t);
     for (int a = 0; a < 7; a++) {
         tc.wx0[a] = (float)wx0[a]; tc.wx2[a] = (float)wx2[a];
         tc.wy0[a] = (float)wy0[a]; tc.wy2[a] = (float)wy2[a];
     }
     const int tiles = k.NY/tc.TY;
     tc.units = (long long)tiles*k.NZ;
-    long long g = tc.units/32;
-    if (g < 1) g = 1;
-    if (g > num_sms) g = num_sms;
-    tc.grid = (int)g;
+    tc.grid = tiles < num_sms ? tiles : num_sms;
     *out = tc;
     return tc.smem_bytes <= 227*1024 ? 0 : -1;
 }
