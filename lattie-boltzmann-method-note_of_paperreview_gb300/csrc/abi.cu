@@ -86,7 +86,7 @@ size_t tables_bytes(const islbm_params &p) {
     const TabSizes s = tab_sizes(p);
     const size_t c = compute_bytes(p.precision);
     return align256(2*s.wx*c) + align256(2*s.wy*c) + align256(s.wxi*c) + align256(s.bq*c) + align256(s.bw*c) +
-           align256(s.flags_bytes) + align256(s.dxv*8) + align256(s.dzv*8);
+           align256(s.flags_bytes) + align256(s.dxv*8) + align256(s.dzv*8) + align256(s.dxv*4) + align256(s.dzv*4);
 }
 
 size_t required_bytes(const islbm_params &p) {
@@ -127,7 +127,7 @@ void pack_tables(const Geometry &g, const islbm_params &p, std::vector<char> &bl
         for (int y = 0; y < NY; y++)
             for (int tt = 0; tt < 8; tt++)
                 for (int a = 0; a < 7; a++)
-                    wxi[((size_t)z*NY + y)*64 + tt*8 + a] = (C)g.XiT[((size_t)tt*7 + a)*nyz + (size_t)(y + 3)*NZ6 + (z + 3)];
+                    wxi[((size_t)z*NY + y)*64 + a*8 + tt] = (C)g.XiT[((size_t)tt*7 + a)*nyz + (size_t)(y + 3)*NZ6 + (z + 3)];
     t.wxi = (const C *)dxi;
     auto [hq, dq] = take(s.bq*sizeof(C));
     for (size_t i = 0; i < s.bq; i++) ((C *)hq)[i] = (C)g.Q[i];
@@ -145,6 +145,12 @@ void pack_tables(const Geometry &g, const islbm_params &p, std::vector<char> &bl
     auto [hdz, ddz] = take(s.dzv*8);
     for (int z = 0; z < NZ; z++) ((double *)hdz)[z] = (g.z[(size_t)0*NZ6 + z + 4] - g.z[(size_t)0*NZ6 + z + 2])/2.0;
     t.dzv = (const double *)ddz;
+    auto [hdxf, ddxf] = take(s.dxv*4);
+    for (int x = 0; x < NX; x++) ((float *)hdxf)[x] = (float)((double *)hdx)[x];
+    t.dxf = (const float *)ddxf;
+    auto [hdzf, ddzf] = take(s.dzv*4);
+    for (int z = 0; z < NZ; z++) ((float *)hdzf)[z] = (float)((double *)hdz)[z];
+    t.dzf = (const float *)ddzf;
     (void)nb;
 }
 

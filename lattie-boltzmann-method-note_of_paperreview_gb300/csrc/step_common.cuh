@@ -6,7 +6,8 @@
 //                two buffers (old/new) swapped every step; storage type S is double, float,
 //                or half/bfloat16 holding the deviation f - w_q;
 //   weights      per-x and per-y Lagrange weights [a][x], [a][y] and the xi weights of the
-//                eight xi tables per (y, z): [(z*NY + y)*64 + t*8 + a] (t = F3,4,5,6,15,16,17,18);
+//                eight xi tables per (y, z), interleaved per stencil point a:
+//                [(z*NY + y)*64 + a*8 + t] (t = F3,4,5,6,15,16,17,18);
 //   BFL tables   flags, Q and the Q < 0.5 weights on the two wall rows, in the reference's
 //                row indexing r = (k-3)*NYD6 + j (C/memory.h:125-145);
 //   controller   body force, rho_modify, bulk-velocity accumulator (FP64, Ctrl below).
@@ -71,12 +72,13 @@ struct Ctrl {
 template <class C> struct Tables {
     const C *wx0, *wx2;        // [a*NX + x], departure x -/+ minSize
     const C *wy0, *wy2;        // [a*NY + y], departure y -/+ minSize
-    const C *wxi;              // [(z*NY + y)*64 + t*8 + a]
+    const C *wxi;              // [(z*NY + y)*64 + a*8 + t]
     const int *bfl_flag;       // [t*nb + r], t: F3, F4, F15, F16; nb = 2*NYD6
     const C *bfl_q;            // [t*nb + r]
     const C *bfl_w;            // [(s*7 + a)*nb + r], s: XB37 XB38 YB378 XiB378 XB49 XB410 YB4910 XiB4910 YB15 XiB15 YB16 XiB16
     const double *dxv;         // [x] (x[i+1]-x[i-1])/2 on the controller plane
     const double *dzv;         // [z] (z[k+1]-z[k-1])/2 on the controller plane
+    const float *dxf, *dzf;    // the same in FP32 (per-column partial sums of the tiled kernel)
 };
 
 struct StepConst {

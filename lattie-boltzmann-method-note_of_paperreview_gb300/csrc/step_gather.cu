@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(128) step_gather_kernel(const S *__restrict__ 
             return load_f<S>(fo + (size_t)q*N, ((size_t)zz*NY + yy)*NX + xx, q);
         };
         const C *wxi = T.wxi + ((size_t)z*NY + y)*64;
-        auto xiw = [&](int t, int c) -> C { return wxi[t*8 + c]; };
+        auto xiw = [&](int t, int c) -> C { return wxi[c*8 + t]; };
         auto wx = [&](const C *tab, int a) -> C { return tab[(size_t)a*NX + x]; };
         auto wy = [&](const C *tab, int b) -> C { return tab[(size_t)b*NY + y]; };
 

@@ -19,6 +19,7 @@
 // Every value of the old populations is read from HBM about once per step (halo rows and
 // segment restarts come from L2); every new value is written once.
 #include <cstring>
+#include <type_traits>
 
 #include "step_common.cuh"
 #include "step_launch.hpp"
@@ -28,8 +29,61 @@ namespace islbm {
 
 namespace {
 
-constexpr int NTHREADS = 256;
-constexpr int NSTAGES = 4;
+constexpr int NTHREADS = 128;
+constexpr int NSTAGES = 2;
+
+// Shared-memory layout of one tile for a spanwise width NXC (a power of two): all offsets are
+// compile-time constants so every shared-memory address is a base plus an immediate.
+//   stage s (NSTAGES of them): population q in [1, 18] as `rows(q)` rows of NXC values
+//   (TY rows, or TY + 6 with the streamwise halo), then the target's xi weights (TY x 64
+//   floats) and f0 row (TY x NXC values); then ybuf [4][TY][NXC] and xbuf [10][TY][NXC] floats,
+//   then the stage mbarriers.
+template <class S, int NXC>
+struct Lay {
+    static constexpr int NX = NXC;
+    static constexpr int TY = NTHREADS/NXC;
+    static constexpr int LOG2NX = NXC == 8 ? 3 : NXC == 16 ? 4 : NXC == 32 ? 5 : NXC == 64 ? 6 : NXC == 128 ? 7 : 8;
+    static constexpr int EB = (int)sizeof(S);
+    static constexpr bool wide(int q) { return q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15; }
+    static constexpr int rows(int q) { return q == 0 ? 0 : (wide(q) ? TY + 6 : TY); }
+    static constexpr int up16(int v) { return (v + 15)/16*16; }
+    static constexpr int off_bytes(int q) {
+        int off = 0;
+        for (int r = 1; r < q; ++r) off = up16(off + rows(r)*NX*EB);
+        return off;
+    }
+    static constexpr int off(int q) { return off_bytes(q)/EB; }
+    static constexpr unsigned pops_bytes() {
+        unsigned b = 0;
+        for (int q = 1; q < 19; ++q) b += (unsigned)(rows(q)*NX*EB);
+        return b;
+    }
+    static constexpr int w_off = off_bytes(19);
+    static constexpr int f0_off = up16(w_off + TY*64*4);
+    static constexpr int stage_bytes = (up16(f0_off + TY*NX*EB) + 127)/128*128;
+    static constexpr unsigned tgt_bytes = (unsigned)(TY*64*4 + TY*NX*EB);
+    static constexpr int ybuf_off = NSTAGES*stage_bytes;
+    static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
+    static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
+    static constexpr int smem_bytes = bar_off + NSTAGES*8;
+};
+
+// packed FP32 pair arithmetic (fma.rn.f32x2)
+struct P2 { unsigned long long v; };
+__device__ __forceinline__ P2 p2(float lo, float hi) {
+    P2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ P2 p2(float2 a) { return p2(a.x, a.y); }
+__device__ __forceinline__ void fma2(P2 &acc, P2 a, P2 b) {
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc.v) : "l"(a.v), "l"(b.v));
+}
+__device__ __forceinline__ float2 unp(P2 a) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a.v));
+    return r;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -87,6 +141,16 @@ template <> __device__ __forceinline__ float4 ld4<__nv_bfloat16>(const __nv_bflo
 }
 template <class S> __device__ __forceinline__ float ld1(const S *p, float w) {
     if constexpr (Storage<S>::dev) return to_c(*p) + w; else return (float)*p;
+}
+// stored value as it is (the deviation f - w for the deviation formats): the interpolation
+// weights of every filter sum to one, so filtering deviations and adding w once at the target
+// equals filtering full values up to rounding
+template <class S> __device__ __forceinline__ float ldv(const S *p) { return (float)to_c(*p); }
+template <class S> __device__ __forceinline__ float2 ldv2(const S *p);
+template <> __device__ __forceinline__ float2 ldv2<float>(const float *p) { return *(const float2 *)p; }
+template <> __device__ __forceinline__ float2 ldv2<__half>(const __half *p) { return __half22float2(*(const __half2 *)p); }
+template <> __device__ __forceinline__ float2 ldv2<__nv_bfloat16>(const __nv_bfloat16 *p) {
+    return __bfloat1622float2(*(const __nv_bfloat162 *)p);
 }
 __device__ __forceinline__ float4 ld4(const float *p) { return *(const float4 *)p; }
 
@@ -157,20 +221,81 @@ __device__ __noinline__ void bfl_node(const S *__restrict__ fo, const Tables<flo
     }
 }
 
-struct Ring {
-    // xi-ring of filtered values, slot k = plane (p - 6 + k); pairs of directions
-    float2 r12[7], r34[7], r56[7], r78[7], r910[7], r1112[7], r1314[7], r1516[7], r1718[7];
-    __device__ __forceinline__ void shift() {
-#pragma unroll
-        for (int s = 0; s < 6; s++) {
-            r12[s] = r12[s + 1]; r34[s] = r34[s + 1]; r56[s] = r56[s + 1]; r78[s] = r78[s + 1]; r910[s] = r910[s + 1];
-            r1112[s] = r1112[s + 1]; r1314[s] = r1314[s + 1]; r1516[s] = r1516[s + 1]; r1718[s] = r1718[s + 1];
-        }
-    }
+// Filtered values of one plane for the node of this thread (pairs of directions).
+struct Slot {
+    float2 r12, r34, r56, r78, r910, r1112, r1314, r1516, r1718;
 };
 
-template <class S, bool LES>
+// xi ring: the 7 planes of the current window in registers, slot (p mod 7) holding plane p.
+// Slot indices are compile-time constants in every access (the 7 window phases are
+// instantiated separately), so the ring is never shifted.
+struct Ring {
+    Slot s[7];
+};
+
+// xi combination of the window whose newest plane sits in slot NEW (oldest in NEW + 1).
+// The 64 weights of (y, z) are interleaved per stencil point c: (xi3, xi4, xi5, xi6, xi15,
+// xi16, xi17, xi18)[c], so one float4 yields the weight pairs of the packed FMAs.
+// Returns F[3..18] and F1, F2 of the plane three below the newest one.
+template <int NEW>
+__device__ __forceinline__ void xi_combine(const Ring &R, const float *wv_, float *F) {
+    const float4 *wv = (const float4 *)wv_;
+    constexpr int O = (NEW + 1) % 7;   // slot of the oldest plane (c = 0)
+    P2 a34 = p2(0.f, 0.f), a56 = a34, a1516 = a34, a1718 = a34, a78 = a34, a910 = a34, a1112 = a34, a1314 = a34;
+#pragma unroll
+    for (int c = 0; c < 7; c++) {
+        const Slot &q = R.s[(O + c) % 7];
+        const float4 w = wv[2*c], u = wv[2*c + 1];
+        fma2(a34, p2(w.x, w.y), p2(q.r34));
+        fma2(a56, p2(w.z, w.w), p2(q.r56));
+        fma2(a1516, p2(u.x, u.y), p2(q.r1516));
+        fma2(a1718, p2(u.z, u.w), p2(q.r1718));
+        fma2(a78, p2(w.x, w.x), p2(q.r78));
+        fma2(a910, p2(w.y, w.y), p2(q.r910));
+        fma2(a1112, p2(w.z, w.z), p2(q.r1112));
+        fma2(a1314, p2(w.w, w.w), p2(q.r1314));
+    }
+    constexpr int MID = (NEW + 4) % 7;   // plane p - 3
+    F[1] = R.s[MID].r12.x; F[2] = R.s[MID].r12.y;
+    float2 t;
+    t = unp(a34); F[3] = t.x; F[4] = t.y;
+    t = unp(a56); F[5] = t.x; F[6] = t.y;
+    t = unp(a78); F[7] = t.x; F[8] = t.y;
+    t = unp(a910); F[9] = t.x; F[10] = t.y;
+    t = unp(a1112); F[11] = t.x; F[12] = t.y;
+    t = unp(a1314); F[13] = t.x; F[14] = t.y;
+    t = unp(a1516); F[15] = t.x; F[16] = t.y;
+    t = unp(a1718); F[17] = t.x; F[18] = t.y;
+}
+
+// the window phase selects the instantiation
+__device__ __forceinline__ void xi_combine_phase(int ph, const Ring &R, const float *wv, float *F) {
+    switch (ph) {
+    case 0: xi_combine<0>(R, wv, F); break;
+    case 1: xi_combine<1>(R, wv, F); break;
+    case 2: xi_combine<2>(R, wv, F); break;
+    case 3: xi_combine<3>(R, wv, F); break;
+    case 4: xi_combine<4>(R, wv, F); break;
+    case 5: xi_combine<5>(R, wv, F); break;
+    default: xi_combine<6>(R, wv, F); break;
+    }
+}
+
+__device__ __forceinline__ void ring_store(Ring &R, int ph, const Slot &v) {
+    switch (ph) {
+    case 0: R.s[0] = v; break;
+    case 1: R.s[1] = v; break;
+    case 2: R.s[2] = v; break;
+    case 3: R.s[3] = v; break;
+    case 4: R.s[4] = v; break;
+    case 5: R.s[5] = v; break;
+    default: R.s[6] = v; break;
+    }
+}
+
+template <class S, bool LES, int NXC>
 struct TiledKernel {
+    using LY = Lay<S, NXC>;
     // per-launch float constants (computed once per thread from the FP64 controller state)
     struct Scal { float f6, f12, rho_mod, tau, lesC; };
     const S *__restrict__ fo;
@@ -182,64 +307,17 @@ struct TiledKernel {
     float *rho_out, *u_out, *v_out, *w_out;
     int macros_on, mass_on;
 
-    // one target node: xi combination, walls, BFL, collision, store. `wv` points at the 64 xi
-    // weights of (y, z) (shared memory for interior targets, global for the wall caps).
-    template <int SLOT12>
-    __device__ __forceinline__ void target(const Ring &R, int x, int y, int z, const float *wv_, float f0, const Scal &sc,
-                                           double &ub, double &mass) const {
-        const int NX = k.NX, NY = k.NY;
+    // Walls, BFL rows, collision and store of one node whose streamed populations are in F
+    // (F[1..18] as filtered values, deviations for the deviation formats; F[0] full).
+    __device__ __forceinline__ void finish(float *F, int x, int y, int z, const Scal &sc, float &ub, float &mass) const {
+        constexpr int NX = LY::NX;
+        const int NY = k.NY;
         const size_t N = (size_t)NX*NY*k.NZ;
         const size_t node = ((size_t)z*NY + y)*NX + x;
-        const float4 *wv = (const float4 *)wv_;
-        float F[19];
-        F[0] = f0;
-        F[1] = R.r12[SLOT12].x; F[2] = R.r12[SLOT12].y;
-        // xi combination, one weight table at a time (8 live weights instead of 56)
-        auto table = [&](int t, float (&w)[7]) {
-            const float4 a = wv[2*t], b = wv[2*t + 1];
-            w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w; w[4] = b.x; w[5] = b.y; w[6] = b.z;
-        };
-        {
-            float w[7];
-            table(XI3, w);
-            float f3 = 0, f7 = 0, f8 = 0;
+        if constexpr (Storage<S>::dev) {
 #pragma unroll
-            for (int c = 0; c < 7; c++) { f3 += w[c]*R.r34[c].x; f7 += w[c]*R.r78[c].x; f8 += w[c]*R.r78[c].y; }
-            F[3] = f3; F[7] = f7; F[8] = f8;
-            table(XI4, w);
-            float f4 = 0, f9 = 0, f10 = 0;
-#pragma unroll
-            for (int c = 0; c < 7; c++) { f4 += w[c]*R.r34[c].y; f9 += w[c]*R.r910[c].x; f10 += w[c]*R.r910[c].y; }
-            F[4] = f4; F[9] = f9; F[10] = f10;
-            table(XI5, w);
-            float f5 = 0, f11 = 0, f12 = 0;
-#pragma unroll
-            for (int c = 0; c < 7; c++) { f5 += w[c]*R.r56[c].x; f11 += w[c]*R.r1112[c].x; f12 += w[c]*R.r1112[c].y; }
-            F[5] = f5; F[11] = f11; F[12] = f12;
-            table(XI6, w);
-            float f6 = 0, f13 = 0, f14 = 0;
-#pragma unroll
-            for (int c = 0; c < 7; c++) { f6 += w[c]*R.r56[c].y; f13 += w[c]*R.r1314[c].x; f14 += w[c]*R.r1314[c].y; }
-            F[6] = f6; F[13] = f13; F[14] = f14;
-            float g = 0;
-            table(XI15, w);
-#pragma unroll
-            for (int c = 0; c < 7; c++) g += w[c]*R.r1516[c].x;
-            F[15] = g; g = 0;
-            table(XI16, w);
-#pragma unroll
-            for (int c = 0; c < 7; c++) g += w[c]*R.r1516[c].y;
-            F[16] = g; g = 0;
-            table(XI17, w);
-#pragma unroll
-            for (int c = 0; c < 7; c++) g += w[c]*R.r1718[c].x;
-            F[17] = g; g = 0;
-            table(XI18, w);
-#pragma unroll
-            for (int c = 0; c < 7; c++) g += w[c]*R.r1718[c].y;
-            F[18] = g;
+            for (int q = 1; q < 19; q++) F[q] += lattice_w<float>(q);
         }
-
         if (z == 0) {
             const S *b = fo + node;
             F[5] = load_f<S>(b + 6*N, 0, 6); F[11] = load_f<S>(b + 14*N, 0, 14); F[12] = load_f<S>(b + 13*N, 0, 13);
@@ -254,34 +332,53 @@ struct TiledKernel {
             const int nb = 2*k.NYD6, r = z*k.NYD6 + (y + 3);
             if (T.bfl_flag[r] | T.bfl_flag[nb + r] | T.bfl_flag[2*nb + r] | T.bfl_flag[3*nb + r]) bfl_node<S>(fo, T, k, x, y, z, F);
         }
-        float rho_s, u1, v1, w1;
-        collide_node<float, LES>(F, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
+        float Fl[19];
 #pragma unroll
-        for (int q = 0; q < 19; q++) store_f<S>(fn + (size_t)q*N, node, q, F[q]);
+        for (int q = 0; q < 19; q++) Fl[q] = F[q];
+        float rho_s, u1, v1, w1;
+        collide_node<float, LES>(Fl, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
+#pragma unroll
+        for (int q = 0; q < 19; q++) store_f<S>(fn + (size_t)q*N, node, q, Fl[q]);
         if (macros_on) { rho_out[node] = rho_s; u_out[node] = u1; v_out[node] = v1; w_out[node] = w1; }
-        if (y == k.yplane) ub += (double)v1*T.dxv[x]*T.dzv[z];
-        if (mass_on) mass += rho_s;
+        // column partials in FP32 (at most NZ terms), folded into FP64 once per column
+        if (y == k.yplane) ub += v1*T.dxf[x]*T.dzf[z];
+        mass += rho_s;
         if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
     }
 
-    // Copies of plane p into one stage: the 18 moving populations (with the streamwise halo
-    // where needed) and, when plane p completes the window of an interior target z = p - 3,
-    // that target's xi weights and f0 row.
+    // F1, F2 of a wall-cap target by direct spanwise gathers (the ring keeps only the plane
+    // three below the newest one)
+    __device__ __forceinline__ void cap_f12(int x, int y, int z, float *F) const {
+        constexpr int NX = LY::NX;
+        const int NY = k.NY;
+        const size_t N = (size_t)NX*NY*k.NZ;
+        const S *r1 = fo + 1*N + ((size_t)z*NY + y)*NX, *r2 = fo + 2*N + ((size_t)z*NY + y)*NX;
+        float a = 0, b = 0;
+#pragma unroll
+        for (int t = 0; t < 7; t++) {
+            const int xx = (x - 3 + t) & (NX - 1);
+            a += tc.wx0[t]*ldv<S>(r1 + xx);
+            b += tc.wx2[t]*ldv<S>(r2 + xx);
+        }
+        F[1] = a; F[2] = b;
+    }
+
     // Issued by warp 0: lane 0 posts the expected bytes, then lane q copies population q
     // (two pieces when the halo wraps) and lanes 19, 20 the target data.
     __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, int lane) const {
-        const int NX = k.NX, NY = k.NY, NZ = k.NZ, TY = tc.TY;
+        constexpr int NX = LY::NX, TY = LY::TY;
+        const int NY = k.NY, NZ = k.NZ;
         const size_t N = (size_t)NX*NY*NZ;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
         const bool tgt = p >= 7 && p <= NZ - 1;
-        if (lane == 0) mbar_expect_tx(bar, tc.stage_bytes_used + (tgt ? tc.tgt_bytes : 0u));
+        if (lane == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         __syncwarp();
         S *pops = (S *)stage;
         const int q = lane;
         if (q >= 1 && q < 19) {
-            S *dst = pops + tc.off[q];
+            S *dst = pops + LY::off(q);
             const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
-            if (tc.rows[q] == TY) {
+            if (!LY::wide(q)) {
                 bulk_g2s(dst, plane_base + (size_t)y0*NX, TY*row_bytes, bar);
             } else {
                 const int ys = y0 >= 3 ? y0 - 3 : y0 - 3 + NY;
@@ -293,11 +390,11 @@ struct TiledKernel {
         }
         if (tgt && lane == 19) {
             const int z = p - 3;
-            bulk_g2s(stage + tc.w_off, T.wxi + ((size_t)z*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
+            bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)z*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
         }
         if (tgt && lane == 20) {
             const int z = p - 3;
-            bulk_g2s(stage + tc.f0_off, fo + ((size_t)z*NY + y0)*NX, TY*row_bytes, bar);
+            bulk_g2s(stage + LY::f0_off, fo + ((size_t)z*NY + y0)*NX, TY*row_bytes, bar);
         }
     }
 
@@ -307,36 +404,36 @@ struct TiledKernel {
         int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
 
-    // One source plane: wait for its copies, advance the ring, filter, store into ring slot 6.
-    __device__ __forceinline__ void plane(int i, int p, int p1, int y0, unsigned char *smem, Ring &R, unsigned &parity,
-                                          bool &faulted, const Lane &L) const {
-        const int NX = k.NX, TY = tc.TY;
+    // One source plane: wait for its copies, filter, return the plane's slot values.
+    __device__ __forceinline__ Slot plane(int i, int p, int p1, int y0, unsigned char *smem, unsigned &parity, bool &faulted,
+                                          const Lane &L) const {
+        constexpr int NX = LY::NX, TY = LY::TY;
         const int s = i % NSTAGES;
-        uint64_t *bars = (uint64_t *)(smem + tc.bar_off);
-        float *ybuf = (float *)(smem + tc.ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
-        float *xbuf = (float *)(smem + tc.xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
-        unsigned char *stage = smem + (size_t)s*tc.stage_bytes;
+        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+        float *ybuf = (float *)(smem + LY::ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
+        float *xbuf = (float *)(smem + LY::xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
+        unsigned char *stage = smem + (size_t)s*LY::stage_bytes;
         const S *raw = (const S *)stage;
         mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted);
         parity ^= 1u << s;
-        R.shift();
+        Slot v;
         {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
-            auto row = [&](int q, int lr) -> const S * { return raw + tc.off[q] + lr*NX + L.xl; };
+            const S *base = raw + L.yl*NX + L.xl;
+            auto row = [&](int q, int b) -> const S * { return base + LY::off(q) + b*NX; };
             float a3 = 0, a4 = 0, a15 = 0, a16 = 0, a17 = 0, a18 = 0, a7 = 0, a8 = 0, a9 = 0, a10 = 0;
 #pragma unroll
             for (int b = 0; b < 7; b++) {
                 const float y0w = tc.wy0[b], y2w = tc.wy2[b];
-                const int lr = L.yl + b;
-                a3 += y0w*ld1<S>(row(3, lr), 1.f/18); a4 += y2w*ld1<S>(row(4, lr), 1.f/18);
-                a15 += y0w*ld1<S>(row(15, lr), 1.f/36); a16 += y2w*ld1<S>(row(16, lr), 1.f/36);
-                a17 += y0w*ld1<S>(row(17, lr), 1.f/36); a18 += y2w*ld1<S>(row(18, lr), 1.f/36);
-                a7 += y0w*ld1<S>(row(7, lr), 1.f/36); a8 += y0w*ld1<S>(row(8, lr), 1.f/36);
-                a9 += y2w*ld1<S>(row(9, lr), 1.f/36); a10 += y2w*ld1<S>(row(10, lr), 1.f/36);
+                a3 += y0w*ldv<S>(row(3, b)); a4 += y2w*ldv<S>(row(4, b));
+                a15 += y0w*ldv<S>(row(15, b)); a16 += y2w*ldv<S>(row(16, b));
+                a17 += y0w*ldv<S>(row(17, b)); a18 += y2w*ldv<S>(row(18, b));
+                a7 += y0w*ldv<S>(row(7, b)); a8 += y0w*ldv<S>(row(8, b));
+                a9 += y2w*ldv<S>(row(9, b)); a10 += y2w*ldv<S>(row(10, b));
             }
-            R.r34[6] = make_float2(a3, a4);
-            R.r1516[6] = make_float2(a15, a16);
-            R.r1718[6] = make_float2(a17, a18);
-            R.r56[6] = make_float2(ld1<S>(row(5, L.yl), 1.f/18), ld1<S>(row(6, L.yl), 1.f/18));
+            v.r34 = make_float2(a3, a4);
+            v.r1516 = make_float2(a15, a16);
+            v.r1718 = make_float2(a17, a18);
+            v.r56 = make_float2(ldv<S>(row(5, 0)), ldv<S>(row(6, 0)));
             const int o = L.yl*NX + L.xl;
             ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
         }
@@ -345,67 +442,77 @@ struct TiledKernel {
         if (L.tid < 32 && p + NSTAGES - 1 <= p1) {
             fence_proxy_async();
             const int sn = (i + NSTAGES - 1) % NSTAGES;
-            issue_plane(smem + (size_t)sn*tc.stage_bytes, &bars[sn], p + NSTAGES - 1, y0, L.tid);
+            issue_plane(smem + (size_t)sn*LY::stage_bytes, &bars[sn], p + NSTAGES - 1, y0, L.tid);
         }
         {   // spanwise filter: two nodes of one row, five directions of one departure side
             const int m = NX - 1;
             const int x0 = L.xx0;
             const int xa = (x0 - 4) & m, xb = (x0 - 2) & m, xc = x0, xd = (x0 + 2) & m, xe = (x0 + 4) & m;
-#pragma unroll
-            for (int j = 0; j < 5; j++) {
+            auto task = [&](auto jc) {
+                constexpr int j = decltype(jc)::value;
                 const int d = 2*j + L.xsel;        // xbuf slot: 7, 8, 9, 10, 1, 2, 11, 12, 13, 14
-                float v[10];
-                if (j < 2) {
+                float vv[10];
+                if constexpr (j < 2) {
                     const float *in = ybuf + (size_t)d*TY*NX + L.xr*NX;
                     const float2 a = *(const float2 *)(in + xa), b = *(const float2 *)(in + xb), c = *(const float2 *)(in + xc),
                                  e = *(const float2 *)(in + xd), g = *(const float2 *)(in + xe);
-                    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = e.x; v[7] = e.y; v[8] = g.x; v[9] = g.y;
+                    vv[0] = a.x; vv[1] = a.y; vv[2] = b.x; vv[3] = b.y; vv[4] = c.x; vv[5] = c.y; vv[6] = e.x; vv[7] = e.y; vv[8] = g.x; vv[9] = g.y;
                 } else {
-                    const int q = d == 4 ? 1 : (d == 5 ? 2 : d + 5);
-                    const float w = q <= 2 ? 1.f/18 : 1.f/36;
-                    const S *in = raw + tc.off[q] + L.xr*NX;
-                    v[0] = ld1<S>(in + xa, w); v[1] = ld1<S>(in + xa + 1, w); v[2] = ld1<S>(in + xb, w); v[3] = ld1<S>(in + xb + 1, w);
-                    v[4] = ld1<S>(in + xc, w); v[5] = ld1<S>(in + xc + 1, w); v[6] = ld1<S>(in + xd, w); v[7] = ld1<S>(in + xd + 1, w);
-                    v[8] = ld1<S>(in + xe, w); v[9] = ld1<S>(in + xe + 1, w);
+                    // population of this task: 1, 11, 13 (xsel 0) or 2, 12, 14 (xsel 1)
+                    constexpr int qa = j == 2 ? 1 : (j == 3 ? 11 : 13);
+                    constexpr int qb = j == 2 ? 2 : (j == 3 ? 12 : 14);
+                    const S *in = raw + (L.xsel ? LY::off(qb) : LY::off(qa)) + L.xr*NX;
+                    const float2 a = ldv2<S>(in + xa), b = ldv2<S>(in + xb), c = ldv2<S>(in + xc), e = ldv2<S>(in + xd),
+                                 g = ldv2<S>(in + xe);
+                    vv[0] = a.x; vv[1] = a.y; vv[2] = b.x; vv[3] = b.y; vv[4] = c.x; vv[5] = c.y; vv[6] = e.x; vv[7] = e.y; vv[8] = g.x; vv[9] = g.y;
                 }
                 float o0 = 0, o1 = 0;
 #pragma unroll
                 for (int a = 0; a < 7; a++) {
                     const float w = L.xsel ? tc.wx2[a] : tc.wx0[a];
-                    o0 += w*v[a + 1]; o1 += w*v[a + 2];
+                    o0 += w*vv[a + 1]; o1 += w*vv[a + 2];
                 }
                 *(float2 *)(xbuf + (size_t)d*TY*NX + L.xr*NX + x0) = make_float2(o0, o1);
-            }
+            };
+            task(std::integral_constant<int, 0>{}); task(std::integral_constant<int, 1>{});
+            task(std::integral_constant<int, 2>{}); task(std::integral_constant<int, 3>{});
+            task(std::integral_constant<int, 4>{});
         }
         __syncthreads();
         {
             const int o = L.yl*NX + L.xl, st = TY*NX;
-            R.r78[6] = make_float2(xbuf[0*st + o], xbuf[1*st + o]);
-            R.r910[6] = make_float2(xbuf[2*st + o], xbuf[3*st + o]);
-            R.r12[6] = make_float2(xbuf[4*st + o], xbuf[5*st + o]);
-            R.r1112[6] = make_float2(xbuf[6*st + o], xbuf[7*st + o]);
-            R.r1314[6] = make_float2(xbuf[8*st + o], xbuf[9*st + o]);
+            v.r78 = make_float2(xbuf[0*st + o], xbuf[1*st + o]);
+            v.r910 = make_float2(xbuf[2*st + o], xbuf[3*st + o]);
+            v.r12 = make_float2(xbuf[4*st + o], xbuf[5*st + o]);
+            v.r1112 = make_float2(xbuf[6*st + o], xbuf[7*st + o]);
+            v.r1314 = make_float2(xbuf[8*st + o], xbuf[9*st + o]);
         }
+        return v;
     }
 
-    template <int SLOT12>
-    __device__ __forceinline__ void cap_target(const Ring &R, int x, int y, int z, const Scal &sc, double &ub,
-                                               double &mass) const {
+    // a wall-cap target: xi weights and f0 from global memory, F1/F2 by direct gathers
+    __device__ __forceinline__ void cap_target(const Ring &R, int ph, int x, int y, int z, const Scal &sc, float &ub,
+                                               float &mass) const {
         const size_t node = ((size_t)z*k.NY + y)*k.NX + x;
-        target<SLOT12>(R, x, y, z, T.wxi + ((size_t)z*k.NY + y)*64, load_f<S>(fo, node, 0), sc, ub, mass);
+        float F[19];
+        xi_combine_phase(ph, R, T.wxi + ((size_t)z*k.NY + y)*64, F);
+        cap_f12(x, y, z, F);
+        F[0] = load_f<S>(fo, node, 0);
+        finish(F, x, y, z, sc, ub, mass);
     }
 
     __device__ void run() const {
         extern __shared__ __align__(128) unsigned char smem[];
-        const int NX = k.NX, NZ = k.NZ, TY = tc.TY;
-        uint64_t *bars = (uint64_t *)(smem + tc.bar_off);
+        constexpr int NX = LY::NX, TY = LY::TY;
+        const int NZ = k.NZ;
+        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         Lane L;
         L.tid = threadIdx.x;
         L.xl = L.tid & (NX - 1);
-        L.yl = L.tid >> tc.log2nx;
-        L.xsel = L.tid >> 7;                           // 128 threads per departure side
-        const int pair = L.tid & 127;                  // TY*NX/2 = 128 node pairs per plane
-        L.xr = pair >> (tc.log2nx - 1);
+        L.yl = L.tid >> LY::LOG2NX;
+        L.xsel = L.tid/(NTHREADS/2);                   // half the threads per departure side
+        const int pair = L.tid & (NTHREADS/2 - 1);     // TY*NX/2 node pairs per plane
+        L.xr = pair >> (LY::LOG2NX - 1);
         L.xx0 = 2*(pair & (NX/2 - 1));
 
         if (L.tid == 0) {
@@ -416,7 +523,7 @@ struct TiledKernel {
         unsigned parity = 0;   // bit s: parity of the next completion of stage s
         bool faulted = false;
 
-        double ub = 0.0, mass = 0.0;
+        double ub_total = 0.0, mass_total = 0.0;
         Scal sc;
         {
             const double force = ctrl->force;
@@ -429,71 +536,61 @@ struct TiledKernel {
         Ring R;
 #pragma unroll
         for (int s = 0; s < 7; s++) {
-            R.r12[s] = R.r34[s] = R.r56[s] = R.r78[s] = R.r910[s] = make_float2(0.f, 0.f);
-            R.r1112[s] = R.r1314[s] = R.r1516[s] = R.r1718[s] = make_float2(0.f, 0.f);
+            const float2 zz = make_float2(0.f, 0.f);
+            R.s[s].r12 = R.s[s].r34 = R.s[s].r56 = R.s[s].r78 = R.s[s].r910 = zz;
+            R.s[s].r1112 = R.s[s].r1314 = R.s[s].r1516 = R.s[s].r1718 = zz;
         }
         // whole columns: CTA b takes tiles b, b + G, b + 2G, ... so that the CTAs running at the
         // same time hold neighbouring tiles at similar heights and share the halo rows in L2
         const int ntiles = k.NY/TY;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            const int za = 0, zb = NZ;
             const int y0 = tile*TY;
-            const int zl = zb - 1;
-            const int p0 = za <= 3 ? 0 : (za >= NZ - 3 ? NZ - 7 : za - 3);
-            const int p1 = zl <= 3 ? 6 : (zl >= NZ - 4 ? NZ - 1 : zl + 3);
-            __syncthreads();   // every thread is done with every stage of the previous segment
+            const int p1 = NZ - 1;
+            __syncthreads();   // every thread is done with every stage of the previous column
             if (L.tid < 32) {
                 fence_proxy_async();
-                for (int s = 0; s < NSTAGES - 1 && p0 + s <= p1; s++)
-                    issue_plane(smem + (size_t)s*tc.stage_bytes, &bars[s], p0 + s, y0, L.tid);
+                for (int s = 0; s < NSTAGES - 1 && s <= p1; s++)
+                    issue_plane(smem + (size_t)s*LY::stage_bytes, &bars[s], s, y0, L.tid);
             }
             const int y = y0 + L.yl;
-            int i = 0, p = p0;
-            // warm-up: the six planes below the first window end
+            float ub = 0.f, mass = 0.f;   // this column's partial sums
+            // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
 #pragma unroll 1
-            for (; i < 6; i++, p++) plane(i, p, p1, y0, smem, R, parity, faulted, L);
-            if (p == 6) {   // window of the lower wall cap (targets 0..3 share planes 0..6)
-                plane(i, p, p1, y0, smem, R, parity, faulted, L);
-                if (za <= 0 && 0 < zb) cap_target<0>(R, L.xl, y, 0, sc, ub, mass);
-                if (za <= 1 && 1 < zb) cap_target<1>(R, L.xl, y, 1, sc, ub, mass);
-                if (za <= 2 && 2 < zb) cap_target<2>(R, L.xl, y, 2, sc, ub, mass);
-                if (za <= 3 && 3 < zb) cap_target<3>(R, L.xl, y, 3, sc, ub, mass);
-                i++; p++;
+            for (int p = 0; p < 7; p++) {
+                const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
+                ring_store(R, p, v);
             }
+            for (int zt = 0; zt < 4; zt++) cap_target(R, 6, L.xl, y, zt, sc, ub, mass);
             // steady state: each plane completes the window of one interior target
-            const int pend = min(p1, NZ - 2);
+            int ph = 0;   // slot of the newest plane = p mod 7
 #pragma unroll 1
-            for (; p <= pend; i++, p++) {
-                plane(i, p, p1, y0, smem, R, parity, faulted, L);
-                const unsigned char *stage = smem + (size_t)(i % NSTAGES)*tc.stage_bytes;
-                const float *wv = (const float *)(stage + tc.w_off) + L.yl*64;
-                const float f0 = ld1<S>((const S *)(stage + tc.f0_off) + L.yl*NX + L.xl, 1.f/3);
-                target<3>(R, L.xl, y, p - 3, wv, f0, sc, ub, mass);
+            for (int p = 7; p <= NZ - 1; p++) {
+                const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
+                ring_store(R, ph, v);
+                const unsigned char *stage = smem + (size_t)(p % NSTAGES)*LY::stage_bytes;
+                const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
+                float F[19];
+                xi_combine_phase(ph, R, wv, F);
+                F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, 1.f/3);
+                finish(F, L.xl, y, p - 3, sc, ub, mass);
+                ph = ph == 6 ? 0 : ph + 1;
             }
-            if (p == NZ - 1 && p <= p1) {   // window of the upper wall cap
-                plane(i, p, p1, y0, smem, R, parity, faulted, L);
-                const int zt = NZ - 4;
-                if (za <= zt && zt < zb) {
-                    const unsigned char *stage = smem + (size_t)(i % NSTAGES)*tc.stage_bytes;
-                    const float *wv = (const float *)(stage + tc.w_off) + L.yl*64;
-                    const float f0 = ld1<S>((const S *)(stage + tc.f0_off) + L.yl*NX + L.xl, 1.f/3);
-                    target<3>(R, L.xl, y, zt, wv, f0, sc, ub, mass);
-                }
-                if (za <= NZ - 3 && NZ - 3 < zb) cap_target<4>(R, L.xl, y, NZ - 3, sc, ub, mass);
-                if (za <= NZ - 2 && NZ - 2 < zb) cap_target<5>(R, L.xl, y, NZ - 2, sc, ub, mass);
-                if (za <= NZ - 1 && NZ - 1 < zb) cap_target<6>(R, L.xl, y, NZ - 1, sc, ub, mass);
-            }
+            // upper cap: targets NZ-3 .. NZ-1 share the last window (newest plane NZ-1)
+            const int phl = (NZ - 1) % 7;
+            for (int zt = NZ - 3; zt < NZ; zt++) cap_target(R, phl, L.xl, y, zt, sc, ub, mass);
+            ub_total += (double)ub;
+            mass_total += (double)mass;
         }
-        end_of_step<NTHREADS>(ctrl, k, tc.n, ub, mass, true, mass_on != 0);
+        end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0);
     }
 };
 
-template <class S, bool LES>
-__global__ void __launch_bounds__(NTHREADS, 1) step_tiled_kernel(TiledKernel<S, LES> K) { K.run(); }
+template <class S, bool LES, int NXC>
+__global__ void __launch_bounds__(NTHREADS, 2) step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
 
-template <class S, bool LES>
+template <class S, bool LES, int NXC>
 cudaError_t launch_t(const StepLaunch &L) {
-    TiledKernel<S, LES> K;
+    TiledKernel<S, LES, NXC> K;
     K.fo = (const S *)L.fo;
     K.fn = (S *)L.fn;
     K.T = *(const Tables<float> *)L.tables;
@@ -504,20 +601,34 @@ cudaError_t launch_t(const StepLaunch &L) {
     K.rho_out = (float *)L.macros[0]; K.u_out = (float *)L.macros[1];
     K.v_out = (float *)L.macros[2]; K.w_out = (float *)L.macros[3];
     K.macros_on = L.macros_on; K.mass_on = L.mass;
-    static size_t attr_smem = 0;   // largest dynamic shared memory enabled for this instantiation
-    const size_t smem = K.tc.smem_bytes;
-    if (smem > attr_smem) {
-        cudaError_t e = cudaFuncSetAttribute(step_tiled_kernel<S, LES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static bool attr_done = false;   // one attribute call per instantiation
+    constexpr size_t smem = Lay<S, NXC>::smem_bytes;
+    if (!attr_done) {
+        cudaError_t e = cudaFuncSetAttribute(step_tiled_kernel<S, LES, NXC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr_smem = smem;
+        attr_done = true;
     }
-    step_tiled_kernel<S, LES><<<K.tc.grid, NTHREADS, smem, L.stream>>>(K);
+    step_tiled_kernel<S, LES, NXC><<<K.tc.grid, NTHREADS, smem, L.stream>>>(K);
     return cudaGetLastError();
+}
+
+template <class S, bool LES>
+cudaError_t launch_nx(const StepLaunch &L) {
+    switch (L.k.NX) {
+    case 32: return launch_t<S, LES, 32>(L);
+    case 64: return launch_t<S, LES, 64>(L);
+    default: return launch_t<S, LES, 128>(L);
+    }
 }
 
 template <class S>
 cudaError_t launch_s(const StepLaunch &L) {
-    return L.les ? launch_t<S, true>(L) : launch_t<S, false>(L);
+    return L.les ? launch_nx<S, true>(L) : launch_nx<S, false>(L);
+}
+
+template <class S>
+size_t smem_for(int nx) {
+    return nx == 32 ? Lay<S, 32>::smem_bytes : (nx == 64 ? Lay<S, 64>::smem_bytes : Lay<S, 128>::smem_bytes);
 }
 
 size_t elem_bytes(int precision) { return precision == ISLBM_FP32 ? 4 : 2; }
@@ -526,8 +637,8 @@ size_t elem_bytes(int precision) { return precision == ISLBM_FP32 ? 4 : 2; }
 
 bool tiled_supported(const StepConst &k, int precision) {
     if (precision == ISLBM_FP64) return false;
-    // NX a power of two in [8, 256] so that a tile is 256 nodes and index math is shifts
-    if (k.NX < 8 || k.NX > NTHREADS || (k.NX & (k.NX - 1)) != 0) return false;
+    // spanwise widths with a compiled layout (a tile is 256 nodes)
+    if (k.NX != 32 && k.NX != 64 && k.NX != 128) return false;
     const int TY = NTHREADS/k.NX;
     if (k.NY % TY != 0 || k.NY < TY + 6 || k.NZ < 8) return false;
     return true;
@@ -563,14 +674,14 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     tc.ybuf_off = NSTAGES*tc.stage_bytes;
     tc.xbuf_off = tc.ybuf_off + (size_t)4*tc.TY*k.NX*sizeof(float);
     tc.bar_off = tc.xbuf_off + (size_t)10*tc.TY*k.NX*sizeof(float);
-    tc.smem_bytes = tc.bar_off + NSTAGES*sizeof(uint64_t);
+    tc.smem_bytes = precision == ISLBM_FP32 ? smem_for<float>(k.NX) : smem_for<__half>(k.NX);
     for (int a = 0; a < 7; a++) {
         tc.wx0[a] = (float)wx0[a]; tc.wx2[a] = (float)wx2[a];
         tc.wy0[a] = (float)wy0[a]; tc.wy2[a] = (float)wy2[a];
     }
     const int tiles = k.NY/tc.TY;
     tc.units = (long long)tiles*k.NZ;
-    tc.grid = tiles < num_sms ? tiles : num_sms;
+    tc.grid = tiles < 2*num_sms ? tiles : 2*num_sms;   // two CTAs per SM
     *out = tc;
     return tc.smem_bytes <= 227*1024 ? 0 : -1;
 }
