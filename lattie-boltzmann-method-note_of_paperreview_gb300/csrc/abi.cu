@@ -16,30 +16,9 @@
 #include "geometry.hpp"
 #include "step_launch.hpp"
 #include "step_tiled.hpp"
+#include "handle.hpp"
 
 using namespace islbm;
-
-struct islbm_handle {
-    islbm_params p{};
-    Geometry g;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    size_t N = 0;
-    size_t elem = 0;           // bytes per stored population value
-    size_t celem = 0;          // bytes per compute-type value
-    void *fbuf[2] = {nullptr, nullptr};
-    void *macros[4] = {nullptr, nullptr, nullptr, nullptr};
-    void *tabmem = nullptr;    // one allocation for all weight tables
-    size_t tab_bytes = 0;
-    Ctrl *ctrl = nullptr;
-    Tables<double> td{};
-    Tables<float> tf{};
-    StepConst k{};
-    int cur = 0;
-    unsigned long long steps = 0;
-    bool use_tiled = false;
-    TiledConst tiled{};
-};
 
 namespace {
 
@@ -247,7 +226,7 @@ int copy_macro(islbm_handle *h, int which, double *out, int layout) {
     return ISLBM_OK;
 }
 
-void free_handle(islbm_handle *h) {
+void free_handle_impl(islbm_handle *h) {
     if (!h) return;
     cudaSetDevice(h->device);
     for (int b = 0; b < 2; b++) if (h->fbuf[b]) cudaFree(h->fbuf[b]);
@@ -357,6 +336,11 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
 
 }  // namespace
 
+namespace islbm {
+int handle_init(const islbm_params *p, islbm_handle *h) { return init_impl(p, h); }
+void handle_free(islbm_handle *h) { free_handle_impl(h); }
+}  // namespace islbm
+
 extern "C" {
 
 int islbm_default_params(islbm_params *p) {
@@ -390,7 +374,7 @@ int islbm_init(const islbm_params *p, islbm_handle **out) {
     islbm_handle *h = new (std::nothrow) islbm_handle();
     if (!h) return ISLBM_ERR_OUT_OF_MEMORY;
     const int st = init_impl(p, h);
-    if (st != ISLBM_OK) { free_handle(h); return st; }
+    if (st != ISLBM_OK) { free_handle_impl(h); return st; }
     *out = h;
     return ISLBM_OK;
 }
@@ -527,7 +511,7 @@ int islbm_check_finite(islbm_handle *h, long long *bad) {
 
 int islbm_destroy(islbm_handle *h) {
     if (!h) return ISLBM_ERR_INVALID_ARGUMENT;
-    free_handle(h);
+    free_handle_impl(h);
     return ISLBM_OK;
 }
 

@@ -1,0 +1,40 @@
+// Device state of one solve (shared by the C ABI and the serving loop).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/islbm.h"
+#include "geometry.hpp"
+#include "step_launch.hpp"
+#include "step_tiled.hpp"
+
+using namespace islbm;
+
+struct islbm_handle {
+    islbm_params p{};
+    Geometry g;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    size_t N = 0;
+    size_t elem = 0;           // bytes per stored population value
+    size_t celem = 0;          // bytes per compute-type value
+    void *fbuf[2] = {nullptr, nullptr};
+    void *macros[4] = {nullptr, nullptr, nullptr, nullptr};
+    void *tabmem = nullptr;    // one allocation for all weight tables
+    size_t tab_bytes = 0;
+    Ctrl *ctrl = nullptr;
+    Tables<double> td{};
+    Tables<float> tf{};
+    StepConst k{};
+    int cur = 0;
+    unsigned long long steps = 0;
+    bool use_tiled = false;
+    TiledConst tiled{};
+};
+
+
+namespace islbm {
+// init/teardown used by the serving loop as well as islbm_init/islbm_destroy
+int handle_init(const islbm_params *p, islbm_handle *h);
+void handle_free(islbm_handle *h);
+}

@@ -182,9 +182,10 @@ __device__ __forceinline__ void finish_step(Ctrl *ctrl, const StepConst &k, unsi
 // finish_step. `ub` and `mass` are this thread's contributions (0 when not applicable).
 // `n` is the 1-based number of the step being computed. `has_plane` must be uniform
 // within a warp (every kernel maps a warp to nodes of one y row).
+// `total` is the number of blocks (or work items) that report to this controller per step.
 template <int NTHREADS>
 __device__ __forceinline__ void end_of_step(Ctrl *ctrl, const StepConst &k, unsigned long long n, double ub,
-                                            double mass, bool has_plane, bool mass_step) {
+                                            double mass, bool has_plane, bool mass_step, unsigned total) {
     __shared__ double red[2][NTHREADS/32];
     __shared__ int any_plane;
     __shared__ bool last;
@@ -215,7 +216,6 @@ __device__ __forceinline__ void end_of_step(Ctrl *ctrl, const StepConst &k, unsi
             atomicAdd(&ctrl->mass_slot[bid & 255u], s);
         }
         __threadfence();
-        const unsigned total = gridDim.x*gridDim.y*gridDim.z;
         last = (atomicAdd(&ctrl->done, 1u) == total - 1u);
     }
     __syncthreads();

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(128) step_gather_kernel(const S *__restrict__ 
         if (MASS) mass = (double)rho_s;
         if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
     }
-    end_of_step<128>(ctrl, k, n, ub, mass, has_plane, MASS);
+    end_of_step<128>(ctrl, k, n, ub, mass, has_plane, MASS, gridDim.x*gridDim.y*gridDim.z);
 }
 
 template <class S, bool LES>

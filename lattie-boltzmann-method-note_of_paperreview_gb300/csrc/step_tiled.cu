@@ -501,11 +501,8 @@ struct TiledKernel {
         finish(F, x, y, z, sc, ub, mass);
     }
 
-    __device__ void run() const {
-        extern __shared__ __align__(128) unsigned char smem[];
-        constexpr int NX = LY::NX, TY = LY::TY;
-        const int NZ = k.NZ;
-        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+    __device__ __forceinline__ Lane lane() const {
+        constexpr int NX = LY::NX;
         Lane L;
         L.tid = threadIdx.x;
         L.xl = L.tid & (NX - 1);
@@ -514,7 +511,65 @@ struct TiledKernel {
         const int pair = L.tid & (NTHREADS/2 - 1);     // TY*NX/2 node pairs per plane
         L.xr = pair >> (LY::LOG2NX - 1);
         L.xx0 = 2*(pair & (NX/2 - 1));
+        return L;
+    }
 
+    __device__ __forceinline__ Scal scalars() const {
+        Scal sc;
+        const double force = ctrl->force;
+        sc.f6 = (float)(1.0/6*force*k.dt);
+        sc.f12 = (float)(1.0/12*force*k.dt);
+        sc.rho_mod = (float)ctrl->rho_modify;
+        sc.tau = (float)k.tau;
+        sc.lesC = (float)k.les_C;
+        return sc;
+    }
+
+    // One whole column (tile rows y0 .. y0+TY-1, all planes): returns its partial sums.
+    __device__ __forceinline__ void column(int tile, unsigned char *smem, Ring &R, unsigned &parity, bool &faulted,
+                                           const Lane &L, const Scal &sc, float &ub, float &mass) const {
+        constexpr int NX = LY::NX, TY = LY::TY;
+        const int NZ = k.NZ;
+        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+        const int y0 = tile*TY;
+        const int p1 = NZ - 1;
+        __syncthreads();   // every thread is done with every stage of the previous column
+        if (L.tid < 32) {
+            fence_proxy_async();
+            for (int s = 0; s < NSTAGES - 1 && s <= p1; s++)
+                issue_plane(smem + (size_t)s*LY::stage_bytes, &bars[s], s, y0, L.tid);
+        }
+        const int y = y0 + L.yl;
+        // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
+#pragma unroll 1
+        for (int p = 0; p < 7; p++) {
+            const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
+            ring_store(R, p, v);
+        }
+        for (int zt = 0; zt < 4; zt++) cap_target(R, 6, L.xl, y, zt, sc, ub, mass);
+        // steady state: each plane completes the window of one interior target
+        int ph = 0;   // slot of the newest plane = p mod 7
+#pragma unroll 1
+        for (int p = 7; p <= NZ - 1; p++) {
+            const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
+            ring_store(R, ph, v);
+            const unsigned char *stage = smem + (size_t)(p % NSTAGES)*LY::stage_bytes;
+            const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
+            float F[19];
+            xi_combine_phase(ph, R, wv, F);
+            F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, 1.f/3);
+            finish(F, L.xl, y, p - 3, sc, ub, mass);
+            ph = ph == 6 ? 0 : ph + 1;
+        }
+        // upper cap: targets NZ-3 .. NZ-1 share the last window (newest plane NZ-1)
+        const int phl = (NZ - 1) % 7;
+        for (int zt = NZ - 3; zt < NZ; zt++) cap_target(R, phl, L.xl, y, zt, sc, ub, mass);
+    }
+
+    __device__ void run() const {
+        extern __shared__ __align__(128) unsigned char smem[];
+        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+        const Lane L = lane();
         if (L.tid == 0) {
             for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
             fence_mbar_init();
@@ -522,71 +577,84 @@ struct TiledKernel {
         __syncthreads();
         unsigned parity = 0;   // bit s: parity of the next completion of stage s
         bool faulted = false;
-
         double ub_total = 0.0, mass_total = 0.0;
-        Scal sc;
-        {
-            const double force = ctrl->force;
-            sc.f6 = (float)(1.0/6*force*k.dt);
-            sc.f12 = (float)(1.0/12*force*k.dt);
-            sc.rho_mod = (float)ctrl->rho_modify;
-            sc.tau = (float)k.tau;
-            sc.lesC = (float)k.les_C;
-        }
+        const Scal sc = scalars();
         Ring R;
-#pragma unroll
-        for (int s = 0; s < 7; s++) {
-            const float2 zz = make_float2(0.f, 0.f);
-            R.s[s].r12 = R.s[s].r34 = R.s[s].r56 = R.s[s].r78 = R.s[s].r910 = zz;
-            R.s[s].r1112 = R.s[s].r1314 = R.s[s].r1516 = R.s[s].r1718 = zz;
-        }
         // whole columns: CTA b takes tiles b, b + G, b + 2G, ... so that the CTAs running at the
         // same time hold neighbouring tiles at similar heights and share the halo rows in L2
-        const int ntiles = k.NY/TY;
+        const int ntiles = k.NY/LY::TY;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            const int y0 = tile*TY;
-            const int p1 = NZ - 1;
-            __syncthreads();   // every thread is done with every stage of the previous column
-            if (L.tid < 32) {
-                fence_proxy_async();
-                for (int s = 0; s < NSTAGES - 1 && s <= p1; s++)
-                    issue_plane(smem + (size_t)s*LY::stage_bytes, &bars[s], s, y0, L.tid);
-            }
-            const int y = y0 + L.yl;
             float ub = 0.f, mass = 0.f;   // this column's partial sums
-            // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
-#pragma unroll 1
-            for (int p = 0; p < 7; p++) {
-                const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
-                ring_store(R, p, v);
-            }
-            for (int zt = 0; zt < 4; zt++) cap_target(R, 6, L.xl, y, zt, sc, ub, mass);
-            // steady state: each plane completes the window of one interior target
-            int ph = 0;   // slot of the newest plane = p mod 7
-#pragma unroll 1
-            for (int p = 7; p <= NZ - 1; p++) {
-                const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
-                ring_store(R, ph, v);
-                const unsigned char *stage = smem + (size_t)(p % NSTAGES)*LY::stage_bytes;
-                const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
-                float F[19];
-                xi_combine_phase(ph, R, wv, F);
-                F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, 1.f/3);
-                finish(F, L.xl, y, p - 3, sc, ub, mass);
-                ph = ph == 6 ? 0 : ph + 1;
-            }
-            // upper cap: targets NZ-3 .. NZ-1 share the last window (newest plane NZ-1)
-            const int phl = (NZ - 1) % 7;
-            for (int zt = NZ - 3; zt < NZ; zt++) cap_target(R, phl, L.xl, y, zt, sc, ub, mass);
+            column(tile, smem, R, parity, faulted, L, sc, ub, mass);
             ub_total += (double)ub;
             mass_total += (double)mass;
         }
-        end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0);
+        end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0,
+                              gridDim.x*gridDim.y*gridDim.z);
     }
+};
+
+// Batched form: one launch advances every solve of a batch (same storage format and spanwise
+// width) by one step. Work items are (solve, tile) pairs; a CTA copies the solve's
+// descriptor into shared memory, takes the old/new buffers from the solve's own step
+// counter (so a graph of identical launches advances the solves step after step), runs the
+// column and reports it to the solve's controller, whose last column closes the step.
+template <class S, bool LES, int NXC>
+struct BatchDesc {
+    TiledKernel<S, LES, NXC> K;
+    S *buf[2];          // population buffers; the old one is buf[step & 1]
+    int ntiles;         // work items of this solve per step
 };
 
 template <class S, bool LES, int NXC>
 __global__ void __launch_bounds__(NTHREADS, 2) step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
+
+template <class S, bool LES, int NXC>
+__global__ void __launch_bounds__(NTHREADS, 2)
+step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const int2 *__restrict__ items, int nitems,
+                        int macros_on) {
+    using KT = TiledKernel<S, LES, NXC>;
+    using LY = Lay<S, NXC>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(16) unsigned char kbuf[sizeof(KT)];
+    __shared__ unsigned long long step_s;
+    KT &K = *(KT *)kbuf;
+    uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    unsigned parity = 0;
+    bool faulted = false;
+    for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+        const int2 w = items[it];   // (solve, tile)
+        __syncthreads();            // previous item done with K and every stage
+        {
+            const unsigned *src = (const unsigned *)&descs[w.x].K;
+            unsigned *dst = (unsigned *)kbuf;
+            for (int i = tid; i < (int)(sizeof(KT)/4); i += NTHREADS) dst[i] = src[i];
+        }
+        if (tid == 0) step_s = *(volatile unsigned long long *)&descs[w.x].K.ctrl->step;
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned long long st = step_s;
+            K.fo = descs[w.x].buf[st & 1ULL];
+            K.fn = descs[w.x].buf[(st + 1) & 1ULL];
+            K.tc.n = st + 1;
+            K.mass_on = K.k.mass_interval > 0 && ((st + 1) % (unsigned long long)K.k.mass_interval) == 0ULL;
+            K.macros_on = macros_on;
+        }
+        __syncthreads();
+        const auto L = K.lane();
+        const auto sc = K.scalars();
+        Ring R;
+        float ub = 0.f, mass = 0.f;
+        K.column(w.y, smem, R, parity, faulted, L, sc, ub, mass);
+        end_of_step<NTHREADS>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
+                              (unsigned)descs[w.x].ntiles);
+    }
+}
 
 template <class S, bool LES, int NXC>
 cudaError_t launch_t(const StepLaunch &L) {
@@ -693,6 +761,90 @@ cudaError_t launch_step_tiled(const StepLaunch &L) {
     case ISLBM_BF16_DEV: return launch_s<__nv_bfloat16>(L);
     default: return cudaErrorNotSupported;
     }
+}
+
+namespace {
+
+template <class T> struct TypeTag { using type = T; };
+
+template <class S, bool LES, int NXC>
+struct BatchOps {
+    using D = BatchDesc<S, LES, NXC>;
+    static size_t bytes() { return sizeof(D); }
+    static void fill(const Tables<float> &T, const StepConst &k, const TiledConst &tc, Ctrl *ctrl, void *const macros[4],
+                     void *buf0, void *buf1, int ntiles, void *out) {
+        D d;
+        std::memset((void *)&d, 0, sizeof(d));
+        d.K.T = T; d.K.k = k; d.K.tc = tc; d.K.ctrl = ctrl;
+        d.K.rho_out = (float *)macros[0]; d.K.u_out = (float *)macros[1];
+        d.K.v_out = (float *)macros[2]; d.K.w_out = (float *)macros[3];
+        d.buf[0] = (S *)buf0; d.buf[1] = (S *)buf1;
+        d.ntiles = ntiles;
+        std::memcpy(out, (const void *)&d, sizeof(d));
+    }
+    static cudaError_t prepare() {
+        static bool attr_done = false;
+        if (!attr_done) {
+            cudaError_t e = cudaFuncSetAttribute(step_tiled_batch_kernel<S, LES, NXC>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)Lay<S, NXC>::smem_bytes);
+            if (e != cudaSuccess) return e;
+            attr_done = true;
+        }
+        return cudaSuccess;
+    }
+    static cudaError_t launch(const void *descs, const int2 *items, int nitems, int grid, int macros_on, cudaStream_t st) {
+        cudaError_t e = prepare();
+        if (e != cudaSuccess) return e;
+        step_tiled_batch_kernel<S, LES, NXC><<<grid, NTHREADS, Lay<S, NXC>::smem_bytes, st>>>((const D *)descs, items,
+                                                                                             nitems, macros_on);
+        return cudaGetLastError();
+    }
+};
+
+template <class F>
+auto dispatch(int precision, int NX, bool les, F &&f) {
+    auto by_nx = [&](auto s_tag, auto les_tag) {
+        using S = typename decltype(s_tag)::type;
+        constexpr bool L = decltype(les_tag)::value;
+        switch (NX) {
+        case 32: return f(BatchOps<S, L, 32>{});
+        case 64: return f(BatchOps<S, L, 64>{});
+        default: return f(BatchOps<S, L, 128>{});
+        }
+    };
+    auto by_les = [&](auto s_tag) {
+        return les ? by_nx(s_tag, std::true_type{}) : by_nx(s_tag, std::false_type{});
+    };
+    switch (precision) {
+    case ISLBM_FP32: return by_les(TypeTag<float>{});
+    case ISLBM_FP16_DEV: return by_les(TypeTag<__half>{});
+    default: return by_les(TypeTag<__nv_bfloat16>{});
+    }
+}
+
+}  // namespace
+
+size_t batch_desc_bytes(int precision, int NX, bool les) {
+    return dispatch(precision, NX, les, [](auto ops) { return decltype(ops)::bytes(); });
+}
+
+void fill_batch_desc(int precision, int NX, bool les, const Tables<float> &T, const StepConst &k, const TiledConst &tc,
+                     Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, void *out) {
+    dispatch(precision, NX, les, [&](auto ops) {
+        decltype(ops)::fill(T, k, tc, ctrl, macros, buf0, buf1, ntiles, out);
+        return 0;
+    });
+}
+
+cudaError_t prepare_step_tiled_batch(int precision, int NX, bool les) {
+    return dispatch(precision, NX, les, [&](auto ops) { return decltype(ops)::prepare(); });
+}
+
+cudaError_t launch_step_tiled_batch(int precision, int NX, bool les, const void *descs, const int2 *items, int nitems,
+                                    int grid, int macros_on, cudaStream_t stream) {
+    return dispatch(precision, NX, les,
+                    [&](auto ops) { return decltype(ops)::launch(descs, items, nitems, grid, macros_on, stream); });
 }
 
 }  // namespace islbm

@@ -55,6 +55,15 @@ class Params(ctypes.Structure):
     ]
 
 
+class SolveInfo(ctypes.Structure):
+    """islbm_solve_info (include/islbm_serve.h)."""
+    _fields_ = [("id", ctypes.c_longlong), ("status", ctypes.c_int), ("steps", ctypes.c_longlong),
+                ("nodes", ctypes.c_longlong), ("delta", ctypes.c_double), ("force", ctypes.c_double),
+                ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
+
+
+SOLVE_STATUS = {0: "queued", 1: "active", 2: "converged", 3: "capped", 4: "diverged", 5: "rejected"}
+
 _lib = None
 
 
@@ -86,6 +95,13 @@ def load():
         "islbm_destroy": [vp],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
+        "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
+        "islbm_server_submit": [vp, P, ctypes.c_longlong, ctypes.c_double, ip, ctypes.POINTER(ctypes.c_longlong)],
+        "islbm_server_pump": [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)],
+        "islbm_server_info": [vp, ctypes.c_longlong, ctypes.POINTER(SolveInfo)],
+        "islbm_server_fields": [vp, ctypes.c_longlong, vp, vp, vp, vp],
+        "islbm_server_stats": [vp, ctypes.POINTER(ctypes.c_longlong), dp, ctypes.POINTER(ctypes.c_size_t)],
+        "islbm_server_destroy": [vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -246,3 +262,65 @@ class Solver:
         if st not in (0, 5):
             check(st)
         return bad.value == 0
+
+
+class Server:
+    """Continuous-batching server over many solves on one GPU (include/islbm_serve.h)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, steps_per_chunk=500):
+        self._L = load()
+        self._s = ctypes.c_void_p()
+        check(self._L.islbm_server_create(device, hbm_budget_bytes, steps_per_chunk, ctypes.byref(self._s)))
+
+    def close(self):
+        if self._s:
+            self._L.islbm_server_destroy(self._s)
+            self._s = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, params, max_steps, tol=0.0, keep_fields=False):
+        rid = ctypes.c_longlong()
+        check(self._L.islbm_server_submit(self._s, ctypes.byref(params), int(max_steps), float(tol), int(keep_fields),
+                                          ctypes.byref(rid)))
+        return rid.value
+
+    def pump(self):
+        a, q = ctypes.c_int(), ctypes.c_int()
+        check(self._L.islbm_server_pump(self._s, ctypes.byref(a), ctypes.byref(q)))
+        return a.value, q.value
+
+    def info(self, rid):
+        i = SolveInfo()
+        check(self._L.islbm_server_info(self._s, rid, ctypes.byref(i)))
+        return {"id": i.id, "status": SOLVE_STATUS.get(i.status, i.status), "steps": i.steps, "nodes": i.nodes,
+                "delta": i.delta, "force": i.force, "t_submit": i.t_submit, "t_admit": i.t_admit, "t_done": i.t_done}
+
+    def fields(self, rid):
+        n = self.info(rid)["nodes"]
+        out = {k: np.empty(n) for k in ("rho", "u", "v", "w")}
+        check(self._L.islbm_server_fields(self._s, rid, *[o.ctypes.data for o in out.values()]))
+        return out
+
+    def stats(self):
+        u, b, m = ctypes.c_longlong(), ctypes.c_double(), ctypes.c_size_t()
+        check(self._L.islbm_server_stats(self._s, ctypes.byref(u), ctypes.byref(b), ctypes.byref(m)))
+        return {"updates": u.value, "busy_seconds": b.value, "bytes_in_use": m.value}
+
+    def drain(self, max_pumps=1_000_000):
+        """Pump until nothing is active or queued."""
+        for _ in range(max_pumps):
+            a, q = self.pump()
+            if a == 0 and q == 0:
+                return
+        raise IslbmError(-1, "server did not drain")

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libislbm_gb300.so")
-SOURCES = ["abi.cu", "geometry.cpp", "step_gather.cu", "step_tiled.cu"]
+SOURCES = ["abi.cu", "geometry.cpp", "step_gather.cu", "step_tiled.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -25,7 +25,7 @@ def nvcc():
 
 def _compile(src, verbose):
     obj = os.path.join(OUT, os.path.basename(src) + ".o")
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "islbm.h")]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", f) for f in ("islbm.h", "islbm_serve.h")]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj, ""
     flags = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

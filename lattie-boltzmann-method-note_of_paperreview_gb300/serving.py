@@ -1,0 +1,119 @@
+"""Request stream for the serving loop: seeded periodic-hill solve requests with Poisson
+arrivals, driven through islbm.Server (continuous batching) or one after another through
+islbm.Solver (sequential plain solves), with completion latency per request.
+
+A request is drawn from its seed: the grid (three sizes of the hill family, named streamwise x
+spanwise x wall-normal), the relaxation time (hence Re_h on that grid), the hill steepness
+alpha and the storage format. Relaxation times are drawn from [0.6, 0.68], the range in which
+the reference step is stable on these grids; Re_h in the thousands puts the reference scheme
+(tau near 1/2) into its divergent range at these resolutions.
+"""
+import time
+
+import numpy as np
+
+import islbm
+
+# (streamwise NY, spanwise NX, wall-normal NZ) and the step cap used for each grid
+GRIDS = [((64, 32, 48), 6000), ((128, 64, 96), 3000), ((256, 128, 192), 1500)]
+
+
+def min_size(NZ, LZ=3.036, CFL=0.6):
+    return (LZ - 1.0) / NZ * CFL
+
+
+def make_requests(n, seed=2024, mean_gap=0.05, precisions=("fp32", "fp16"), tol=1e-5, cap_scale=1.0):
+    """n requests with exponential inter-arrival gaps (mean `mean_gap` seconds)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(mean_gap)
+        (ny, nx, nz), cap = GRIDS[rng.integers(len(GRIDS))]
+        tau = rng.uniform(0.6, 0.68)
+        alpha = rng.uniform(0.8, 1.2)
+        prec = precisions[rng.integers(len(precisions))]
+        ub = 0.05
+        re = 3.0 * ub / ((tau - 0.5) * min_size(nz))
+        out.append(dict(arrival=t, NX=nx, NY=ny, NZ=nz, Re=re, Uref=ub, alpha=alpha, precision=prec,
+                        seed=int(rng.integers(1, 2**31)), max_steps=max(1, int(cap * cap_scale)), tol=tol))
+    return out
+
+
+def params_of(req, **override):
+    kw = dict(NX=req["NX"], NY=req["NY"], NZ=req["NZ"], Re=req["Re"], Uref=req["Uref"], alpha=req["alpha"],
+              precision=req["precision"], seed=req["seed"], init_mode=1, perturb=0.01, NDTFRC=100)
+    kw.update(override)
+    return islbm.default_params(**kw)
+
+
+def _stats(lat):
+    lat = np.sort(np.asarray(lat))
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "max_s": float(lat.max())}
+
+
+def run_server(reqs, steps_per_chunk=500, hbm_budget_bytes=150 << 30, device=0, keep=()):
+    """Submit each request at its arrival time, pump until all retired. Returns a summary and the
+    per-request info (fields of the request indices in `keep` are kept)."""
+    with islbm.Server(device=device, hbm_budget_bytes=hbm_budget_bytes, steps_per_chunk=steps_per_chunk) as srv:
+        t0 = time.monotonic()
+        pending = list(range(len(reqs)))
+        ids, lag = {}, {}
+        infos, fields = {}, {}
+        while True:
+            now = time.monotonic() - t0
+            while pending and reqs[pending[0]]["arrival"] <= now:
+                i = pending.pop(0)
+                r = reqs[i]
+                ids[i] = srv.submit(params_of(r), r["max_steps"], r["tol"], keep_fields=i in keep)
+                lag[i] = (time.monotonic() - t0) - r["arrival"]
+            active, queued = srv.pump()
+            if active == 0 and queued == 0:
+                if not pending:
+                    break
+                time.sleep(max(0.0, reqs[pending[0]]["arrival"] - (time.monotonic() - t0)))
+        wall = time.monotonic() - t0
+        lat = []
+        for i, rid in ids.items():
+            inf = srv.info(rid)
+            infos[i] = inf
+            lat.append(inf["t_done"] - inf["t_submit"] + lag[i])
+            if i in keep:
+                fields[i] = srv.fields(rid)
+        st = srv.stats()
+    first = min(r["arrival"] for r in reqs)
+    return {"updates": st["updates"], "wall_s": wall, "busy_s": st["busy_seconds"],
+            "mlups": st["updates"] / max(wall - first, 1e-9) / 1e6, "latency": _stats(lat),
+            "status": {s: sum(1 for v in infos.values() if v["status"] == s) for s in islbm.SOLVE_STATUS.values()}}, \
+        infos, fields
+
+
+def run_sequential(reqs, steps_per_check=500, device=0):
+    """The same requests as plain solves, one at a time in arrival order (each starts at its arrival or
+    when the previous one ends), with the same convergence check every `steps_per_check` steps."""
+    t0 = time.monotonic()
+    lat, updates = [], 0
+    for r in reqs:
+        now = time.monotonic() - t0
+        if now < r["arrival"]:
+            time.sleep(r["arrival"] - now)
+        with islbm.Solver(params_of(r, device=device)) as s:
+            n = r["NX"] * r["NY"] * r["NZ"]
+            prev = None
+            steps = 0
+            while steps < r["max_steps"]:
+                k = min(steps_per_check, r["max_steps"] - steps)
+                s.step(k)
+                steps += k
+                f = s.fields()
+                u = np.stack([f["u"], f["v"], f["w"]])
+                if prev is not None and np.sqrt(np.sum((u - prev) ** 2) / n) / r["Uref"] < r["tol"]:
+                    break
+                prev = u
+            updates += steps * n
+        lat.append(time.monotonic() - t0 - r["arrival"])
+    wall = time.monotonic() - t0
+    first = min(r["arrival"] for r in reqs)
+    return {"updates": updates, "wall_s": wall, "mlups": updates / max(wall - first, 1e-9) / 1e6,
+            "latency": _stats(lat)}

@@ -1,4 +1,4 @@
-"""C ABI of libislbm_gb300.so: every symbol of include/islbm.h is exported, argument checks
+"""C ABI of libislbm_gb300.so: every symbol declared in include/*.h is exported, argument checks
 return status codes, and sizes are computed without a device."""
 import ctypes
 import os
@@ -10,14 +10,15 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "islbm.h")).read()
+    inc = os.path.join(ROOT, "include")
+    src = "".join(open(os.path.join(inc, f)).read() for f in sorted(os.listdir(inc)) if f.endswith(".h"))
     return sorted(set(re.findall(r"ISLBM_API\s+(?:const\s+)?\w+\s*\*?\s*(islbm_\w+)\s*\(", src)))
 
 
 def test_all_declared_symbols_exported(islbm_lib):
     lib = ctypes.CDLL(islbm_lib.LIB_PATH)
     names = declared_symbols()
-    assert len(names) >= 18
+    assert len(names) >= 25
     for n in names:
         assert hasattr(lib, n), n
 
@@ -62,3 +63,12 @@ def test_status_strings(islbm_lib):
     L = islbm_lib.load()
     for s in range(8):
         assert L.islbm_status_string(s)
+
+
+def test_server_argument_checks(islbm_lib):
+    L = islbm_lib.load()
+    s = ctypes.c_void_p()
+    assert L.islbm_server_create(0, 0, 0, ctypes.byref(s)) == 1      # steps_per_chunk < 1
+    assert L.islbm_server_pump(None, None, None) == 1
+    assert L.islbm_server_destroy(None) == 1
+    assert L.islbm_server_submit(None, None, 1, 0.0, 0, None) == 1
