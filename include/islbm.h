@@ -137,6 +137,14 @@ ISLBM_API int islbm_sync(islbm_handle *h);
 /* Count non-finite values in the current state (0 = healthy). */
 ISLBM_API int islbm_check_finite(islbm_handle *h, long long *bad);
 
+/* Whole-field diagnostics from the current populations (FP64 reduction over unique nodes):
+ * out[0] total mass sum(rho), out[1] mean streamwise momentum sum(rho v)/N, out[2] kinetic
+ * energy sum(rho |u|^2)/2, out[3] maximum speed max|u|. Replaces the host-side mass check of
+ * the reference main loop (all populations copied by SendDataToCPU, C/communication.h:260-273,
+ * every 100 steps) and extends the Monitor.dat record (C/monitor.h:4-26). Allocates a scratch
+ * buffer of 512 + 32*ceil(N/2048) bytes on the device for the call and frees it. */
+ISLBM_API int islbm_diagnostics(islbm_handle *h, double *out);
+
 ISLBM_API int islbm_destroy(islbm_handle *h);
 
 ISLBM_API const char *islbm_status_string(int status);

@@ -339,6 +339,7 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
 namespace islbm {
 int handle_init(const islbm_params *p, islbm_handle *h) { return init_impl(p, h); }
 void handle_free(islbm_handle *h) { free_handle_impl(h); }
+int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
 }  // namespace islbm
 
 extern "C" {

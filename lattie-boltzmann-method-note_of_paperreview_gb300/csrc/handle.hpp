@@ -37,4 +37,6 @@ namespace islbm {
 // init/teardown used by the serving loop as well as islbm_init/islbm_destroy
 int handle_init(const islbm_params *p, islbm_handle *h);
 void handle_free(islbm_handle *h);
+// record a CUDA failure for islbm_status_string and map it to a status
+int report_cuda(cudaError_t e, const char *what);
 }

@@ -2,22 +2,24 @@
 //
 // Same step as stream_collide (C/evolution.h:358-684) for FP32 arithmetic with FP32, FP16 or
 // BF16 population storage, organised for HBM:
-//   * a CTA owns a tile of TY full-width rows (all NX spanwise nodes, TY streamwise rows) and
-//     marches upward through the wall-normal planes; every plane of the 18 moving
+//   * a CTA owns a tile of TY = 128/NX full-width rows (all NX spanwise nodes) and marches
+//     upward through the wall-normal planes of that column; every plane of the 18 moving
 //     populations is copied global -> shared with cp.async.bulk (one copy per population and
 //     plane, 3-row streamwise halo for the ten populations with e_y != 0, periodic wrap by
-//     splitting the copy), tracked by an mbarrier, 3 stages deep;
+//     splitting the copy), tracked by an mbarrier, 2 stages deep; the target plane's xi
+//     weights and f0 row ride in the same stage;
 //   * the interpolation is applied as separable filters, exact in real arithmetic because the
 //     x and y weights are the same for every node (uniform spacing, C/initialization.h:51-108)
 //     and the xi weights depend only on the target (y, z): a streamwise filter over the halo
-//     rows, then a spanwise filter (4 nodes per task) through shared memory, then the xi
-//     combination over a 7-plane ring of filtered values kept in registers, so each loaded
-//     value feeds 7 target planes without being re-read;
+//     rows, then a spanwise filter (2 nodes per task) through shared memory, then the xi
+//     combination over a 7-plane ring of filtered values kept in registers (packed FP32x2
+//     FMAs), so each loaded value feeds 7 target planes without being re-read;
 //   * the collision tail, wall bounce-back, BFL rows and controller partial sums are fused;
-//   * CTAs are persistent (one per SM) and split the flattened (tile, z) work evenly; a
-//     segment that starts inside a column first re-reads the 6 planes below it.
-// Every value of the old populations is read from HBM about once per step (halo rows and
-// segment restarts come from L2); every new value is written once.
+//   * CTAs are persistent (2 per SM, 128 threads each) and take whole columns: CTA b takes
+//     tiles b, b + G, b + 2G, ..., so CTAs running at the same time hold neighbouring tiles at
+//     similar heights and share the streamwise halo rows through L2.
+// Every value of the old populations is read from HBM about once per step (halo rows come
+// from L2); every new value is written once.
 #include <cstring>
 #include <type_traits>
 
@@ -105,18 +107,25 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
     return ok != 0;
 }
 // Bounded wait: gives up after about a second, records the fault and lets the kernel run
-// to its end (no thread can be left behind at a barrier).
+// to its end (no thread can be left behind at a barrier). Returns whether the phase completed.
 // After one timeout the thread stops waiting altogether (`faulted`), so a broken pipeline
-// costs one bounded wait, not one per plane.
-__device__ __forceinline__ void mbar_wait(uint64_t *bar, unsigned parity, Ctrl *ctrl, bool &faulted) {
-    if (faulted) return;
+// costs one bounded wait, not one per plane; warp 0 then starts no further copies and, at
+// the end of the kernel, waits (bounded again) for the copies it had started.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, Ctrl *ctrl, bool &faulted) {
+    if (faulted) return false;
     for (int it = 0; it < (1 << 22); ++it) {
-        if (mbar_try_wait(bar, parity)) return;
+        if (mbar_try_wait(bar, parity)) return true;
         if (it > 32) __nanosleep(256);
     }
     faulted = true;
     atomicOr(&ctrl->fault, 1u);
+    return false;
 }
+
+// Pipeline word kept by every thread: bit s = parity of the next completion of stage s;
+// bit PEND + s = warp 0 started a copy on stage s that it has not seen complete;
+// bit PPAR + s = the completion parity of that copy.
+constexpr int PEND = 8, PPAR = 16;
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(dst)),
@@ -398,11 +407,36 @@ struct TiledKernel {
         }
     }
 
+    // Warp 0, at the end of the kernel: bounded wait for copies still pending (only after a
+    // timeout; in a healthy run every copy has been consumed).
+    __device__ __forceinline__ void drain(unsigned char *smem, unsigned parity, int tid) const {
+        if (tid >= 32) return;
+        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
+        for (int s = 0; s < NSTAGES; s++) {
+            if (!((parity >> (PEND + s)) & 1u)) continue;
+            const unsigned ph = (parity >> (PPAR + s)) & 1u;
+            for (int it = 0; it < (1 << 22); ++it) {
+                if (mbar_try_wait(&bars[s], ph)) break;
+                if (it > 32) __nanosleep(256);
+            }
+        }
+    }
+
     struct Lane {
         int tid, xl, yl;        // node of this thread within the tile
         int xr, xx0;            // spanwise-filter task: row and first of two nodes
         int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
+
+    // Warp 0: start the copies of plane p into stage s and record them as pending. After a
+    // timed-out wait in any lane of warp 0 no new copy is started.
+    __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity,
+                                          bool faulted) const {
+        if (__any_sync(0xffffffffu, faulted)) return;
+        fence_proxy_async();
+        issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, y0, L.tid);
+        parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
+    }
 
     // One source plane: wait for its copies, filter, return the plane's slot values.
     __device__ __forceinline__ Slot plane(int i, int p, int p1, int y0, unsigned char *smem, unsigned &parity, bool &faulted,
@@ -414,7 +448,7 @@ struct TiledKernel {
         float *xbuf = (float *)(smem + LY::xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
         unsigned char *stage = smem + (size_t)s*LY::stage_bytes;
         const S *raw = (const S *)stage;
-        mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted);
+        if (mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted)) parity &= ~(1u << (PEND + s));
         parity ^= 1u << s;
         Slot v;
         {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
@@ -439,11 +473,7 @@ struct TiledKernel {
         }
         __syncthreads();
         // every thread has finished plane i-1: its stage can take plane i + NSTAGES - 1
-        if (L.tid < 32 && p + NSTAGES - 1 <= p1) {
-            fence_proxy_async();
-            const int sn = (i + NSTAGES - 1) % NSTAGES;
-            issue_plane(smem + (size_t)sn*LY::stage_bytes, &bars[sn], p + NSTAGES - 1, y0, L.tid);
-        }
+        if (L.tid < 32 && p + NSTAGES - 1 <= p1) issue(smem, (i + NSTAGES - 1) % NSTAGES, p + NSTAGES - 1, y0, L, parity, faulted);
         {   // spanwise filter: two nodes of one row, five directions of one departure side
             const int m = NX - 1;
             const int x0 = L.xx0;
@@ -534,11 +564,8 @@ struct TiledKernel {
         const int y0 = tile*TY;
         const int p1 = NZ - 1;
         __syncthreads();   // every thread is done with every stage of the previous column
-        if (L.tid < 32) {
-            fence_proxy_async();
-            for (int s = 0; s < NSTAGES - 1 && s <= p1; s++)
-                issue_plane(smem + (size_t)s*LY::stage_bytes, &bars[s], s, y0, L.tid);
-        }
+        if (L.tid < 32)
+            for (int s = 0; s < NSTAGES - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity, faulted);
         const int y = y0 + L.yl;
         // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
 #pragma unroll 1
@@ -589,6 +616,7 @@ struct TiledKernel {
             ub_total += (double)ub;
             mass_total += (double)mass;
         }
+        drain(smem, parity, L.tid);
         end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0,
                               gridDim.x*gridDim.y*gridDim.z);
     }
@@ -654,6 +682,8 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         end_of_step<NTHREADS>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
                               (unsigned)descs[w.x].ntiles);
     }
+    __syncthreads();
+    if (nitems > 0) K.drain(smem, parity, tid);
 }
 
 template <class S, bool LES, int NXC>

@@ -93,6 +93,7 @@ def load():
         "islbm_sync": [vp],
         "islbm_check_finite": [vp, ctypes.POINTER(ctypes.c_longlong)],
         "islbm_destroy": [vp],
+        "islbm_diagnostics": [vp, dp],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
@@ -256,6 +257,12 @@ class Solver:
         check(self._L.islbm_get_stream(self._h, ctypes.byref(s)))
         return s.value or 0
 
+    def diagnostics(self):
+        """Total mass, mean streamwise momentum, kinetic energy and maximum speed (FP64)."""
+        out = (ctypes.c_double * 4)()
+        check(self._L.islbm_diagnostics(self._h, out))
+        return {"mass": out[0], "momentum_y": out[1], "kinetic_energy": out[2], "max_speed": out[3]}
+
     def healthy(self):
         bad = ctypes.c_longlong()
         st = self._L.islbm_check_finite(self._h, ctypes.byref(bad))
@@ -270,6 +277,7 @@ class Server:
     def __init__(self, device=0, hbm_budget_bytes=0, steps_per_chunk=500):
         self._L = load()
         self._s = ctypes.c_void_p()
+        self._dims = {}
         check(self._L.islbm_server_create(device, hbm_budget_bytes, steps_per_chunk, ctypes.byref(self._s)))
 
     def close(self):
@@ -293,6 +301,7 @@ class Server:
         rid = ctypes.c_longlong()
         check(self._L.islbm_server_submit(self._s, ctypes.byref(params), int(max_steps), float(tol), int(keep_fields),
                                           ctypes.byref(rid)))
+        self._dims[rid.value] = (params.NZ, params.NY, params.NX)
         return rid.value
 
     def pump(self):
@@ -307,8 +316,8 @@ class Server:
                 "delta": i.delta, "force": i.force, "t_submit": i.t_submit, "t_admit": i.t_admit, "t_done": i.t_done}
 
     def fields(self, rid):
-        n = self.info(rid)["nodes"]
-        out = {k: np.empty(n) for k in ("rho", "u", "v", "w")}
+        """rho, u, v, w of a request, each shaped (NZ, NY, NX) (unique-node layout)."""
+        out = {k: np.empty(self._dims[rid]) for k in ("rho", "u", "v", "w")}
         check(self._L.islbm_server_fields(self._s, rid, *[o.ctypes.data for o in out.values()]))
         return out
 
