@@ -25,3 +25,13 @@ def test_diverges_at_re_700_from_rest(oracle_mod):
     late = np.abs(o.unique(o.get("rho")) - 1).max()
     assert early < 1e-3
     assert not (late < 1.0)   # grown by orders of magnitude (or non-finite)
+
+
+def test_diverges_when_only_the_horizontal_grid_is_refined(oracle_mod):
+    # same wall-normal grid and tau = 0.6 as the stable case, twice the spanwise and streamwise
+    # resolution: the departure offsets in x/y grid units double and the step blows up
+    re = 3 * 0.05 / (0.1 * min_size(48))
+    o = oracle_mod.Oracle(64, 128, 48, re=re, ndtfrc=50, init_mode=1, seed=7)
+    o.step(70)
+    rho = o.unique(o.get("rho"))
+    assert not (np.abs(rho - 1).max() < 1.0)
