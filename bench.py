@@ -186,7 +186,8 @@ def serve_run(islbm, nreq, device):
                      "rel_l2_u_vs_fp64": rel_l2(np.stack([g[c] for c in "uvw"]), np.stack([ref[c] for c in "uvw"])),
                      "max_abs_u_over_ub": float(max(np.abs(g[c] - ref[c]).max() for c in "uvw") / r["Uref"])})
     return {"requests": nreq, "mean_gap_s": 0.05, "grids": "64x32x48 / 128x64x96 / 256x128x192 (NY x NX x NZ)",
-            "steps_cap": {str(g): c for g, c in serving.GRIDS}, "tau_range": [0.6, 0.68], "alpha_range": [0.8, 1.2],
+            "steps_cap": {"x".join(map(str, g)): c for g, c, _ in serving.GRIDS},
+            "tau_range": {"x".join(map(str, g)): list(t) for g, _, t in serving.GRIDS}, "alpha_range": [0.8, 1.2],
             "tol": reqs[0]["tol"], "chunk": 500,
             "server": srv, "sequential": seq, "speedup_mlups": srv["mlups"] / seq["mlups"],
             "error_vs_fp64": errs}

@@ -24,7 +24,7 @@ def alone(islbm, p, steps):
 
 # (precision, NX, les, tau): batched groups (FP32 / FP16, two widths, LES on/off) plus an FP64
 # solve that runs on its own kernel inside the same pump
-MIX = [("fp32", 32, 0.0, 0.60), ("fp32", 32, 0.0, 0.65), ("fp32", 64, 0.0, 0.60),
+MIX = [("fp32", 32, 0.0, 0.60), ("fp32", 32, 0.0, 0.65), ("fp32", 64, 0.0, 0.90),
        ("fp16", 32, 0.0, 0.62), ("fp32", 32, 0.1, 0.60), ("fp64", 32, 0.0, 0.60)]
 TOL = {"fp64": 1e-12, "fp32": 1e-6, "fp16": 1e-4}
 
@@ -32,8 +32,8 @@ TOL = {"fp64": 1e-12, "fp32": 1e-6, "fp16": 1e-4}
 def test_same_alone_and_in_mix(islbm_lib):
     islbm = islbm_lib
     steps = 230   # not a multiple of the chunk: the last chunk is shorter
-    # the hill-grid family (NY, NX, NZ) = (2, 1, 3/2) * NX keeps the departure offsets in grid
-    # units fixed; the reference scheme diverges on 64 x 128 x 48 at tau = 0.6
+    # grids of the hill family (NY, NX, NZ) = (2, 1, 3/2) * NX; the reference scheme needs a
+    # larger tau on the finer grid (it diverges on 64 x 128 x 96 at tau = 0.6 and 0.7)
     params = [stable(islbm, NX=nx, NY=2 * nx, NZ=3 * nx // 2, tau=tau, precision=prec, les_cs=cs)
               for prec, nx, cs, tau in MIX]
     with islbm.Server(steps_per_chunk=100) as srv:
