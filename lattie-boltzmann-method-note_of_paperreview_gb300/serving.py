@@ -110,7 +110,9 @@ def run_sequential(reqs, steps_per_check=500, device=0):
                 steps += k
                 f = s.fields()
                 u = np.stack([f["u"], f["v"], f["w"]])
-                if np.sqrt(np.sum((u - prev) ** 2) / n) / r["Uref"] < r["tol"]:
+                delta = np.sqrt(np.sum((u - prev) ** 2) / n) / r["Uref"]
+                # the server's retirement rules: converged, or diverged (non-finite or delta > 1000)
+                if delta < r["tol"] or not (delta <= 1e3):
                     break
                 prev = u
             updates += steps * n
