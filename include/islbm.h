@@ -145,6 +145,17 @@ ISLBM_API int islbm_check_finite(islbm_handle *h, long long *bad);
  * every 100 steps) and extends the Monitor.dat record (C/monitor.h:4-26). Allocates a scratch
  * buffer of 512 + 32*ceil(N/2048) bytes on the device for the call and frees it. */
 ISLBM_API int islbm_diagnostics(islbm_handle *h, double *out);
+/* The same diagnostics without any device allocation. No reference counterpart: the reference
+ * has no such call. It is for callers that cannot allocate device memory during a run: a
+ * serving loop whose device budget is committed to the byte, or code that must not call
+ * cudaFree (it waits for all work on the device). Instead of a per-call buffer it uses one
+ * fixed scratch array of 524,800 bytes in device memory (per device), so it serves grids of
+ * at most 33,554,432 nodes (NX*NY*NZ); larger grids get ISLBM_ERR_NOT_SUPPORTED with a message,
+ * and islbm_diagnostics serves them. The first call on a device looks up the scratch address
+ * on that device (cudaGetSymbolAddress): make that first call before any stream capture.
+ * Calls that overlap in time (other threads, or other handles on the same device) share the
+ * scratch and race: run them one at a time. */
+ISLBM_API int islbm_diagnostics_noalloc(islbm_handle *h, double *out);
 
 ISLBM_API int islbm_destroy(islbm_handle *h);
 

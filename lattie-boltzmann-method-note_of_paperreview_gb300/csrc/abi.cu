@@ -345,6 +345,10 @@ namespace islbm {
 int handle_init(const islbm_params *p, islbm_handle *h) { return init_impl(p, h); }
 void handle_free(islbm_handle *h) { free_handle_impl(h); }
 int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+int report_status(int status, const char *msg) {
+    g_last = msg;
+    return status;
+}
 }  // namespace islbm
 
 extern "C" {

@@ -16,6 +16,8 @@
 // the result does not depend on scheduling, and writes it to scratch.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 #include "handle.hpp"
 
@@ -116,8 +118,22 @@ cudaError_t launch_diag(const islbm_handle *h, unsigned char *scratch, cudaStrea
     return cudaGetLastError();
 }
 
+// Limits of islbm_diagnostics_noalloc: DIAG_NOALLOC_MAX_BLOCKS reduction blocks of 2048 nodes.
+constexpr size_t DIAG_NOALLOC_MAX_BLOCKS = 16384;
+constexpr size_t DIAG_NOALLOC_MAX_NODES = DIAG_NOALLOC_MAX_BLOCKS*DIAG_NODES_PER_BLOCK;   // 33,554,432
+constexpr size_t DIAG_NOALLOC_BYTES = DIAG_PARTIAL_OFF + 32*DIAG_NOALLOC_MAX_BLOCKS;      // 524,800
+constexpr int DIAG_MAX_DEVICES = 64;
+
 }  // namespace
 }  // namespace islbm
+
+// Scratch of islbm_diagnostics_noalloc: one fixed array in device memory (one copy per device).
+static __device__ __align__(256) unsigned char g_diag_scratch[islbm::DIAG_NOALLOC_BYTES];
+
+// Device address of g_diag_scratch per device: in host code the symbol name is not a device
+// address, so it is looked up once per device, with that device current.
+static std::mutex g_diag_mu;
+static unsigned char *g_diag_ptr[islbm::DIAG_MAX_DEVICES] = {};
 
 using namespace islbm;
 
@@ -135,5 +151,37 @@ extern "C" int islbm_diagnostics(islbm_handle *h, double *out) {
     const cudaError_t ef = cudaFree(scratch);
     if (e != cudaSuccess) return report_cuda(e, "diagnostics");
     if (ef != cudaSuccess) return report_cuda(ef, "cudaFree(diagnostics scratch)");
+    return ISLBM_OK;
+}
+
+// No-allocation variant of islbm_diagnostics: the same kernel on a fixed scratch array.
+extern "C" int islbm_diagnostics_noalloc(islbm_handle *h, double *out) {
+    if (!h || !out) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (h->N > DIAG_NOALLOC_MAX_NODES) {
+        const std::string msg = "islbm_diagnostics_noalloc: the grid has " + std::to_string(h->N) +
+                                " nodes; its fixed scratch holds at most " + std::to_string(DIAG_NOALLOC_MAX_NODES) +
+                                " (use islbm_diagnostics)";
+        return report_status(ISLBM_ERR_NOT_SUPPORTED, msg.c_str());
+    }
+    if (h->device < 0 || h->device >= DIAG_MAX_DEVICES) return report_status(ISLBM_ERR_NOT_SUPPORTED, "device index too large");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    unsigned char *scratch = nullptr;
+    {
+        // set-up on the first call on this device, with the device current
+        std::lock_guard<std::mutex> lock(g_diag_mu);
+        if (!g_diag_ptr[h->device]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_diag_scratch);
+            if (e != cudaSuccess) return report_cuda(e, "cudaGetSymbolAddress(diagnostics scratch)");
+            g_diag_ptr[h->device] = (unsigned char *)p;
+        }
+        scratch = g_diag_ptr[h->device];
+    }
+    e = cudaMemsetAsync(scratch, 0, DIAG_RESULT_OFF, h->stream);   // the done counter starts at zero
+    if (e == cudaSuccess) e = launch_diag(h, scratch, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, scratch + DIAG_RESULT_OFF, 4*sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return report_cuda(e, "diagnostics (no allocation)");
     return ISLBM_OK;
 }

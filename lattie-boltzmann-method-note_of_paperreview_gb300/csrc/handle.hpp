@@ -40,4 +40,6 @@ int handle_init(const islbm_params *p, islbm_handle *h);
 void handle_free(islbm_handle *h);
 // record a CUDA failure for islbm_status_string and map it to a status
 int report_cuda(cudaError_t e, const char *what);
+// record a message for islbm_status_string and return `status`
+int report_status(int status, const char *msg);
 }

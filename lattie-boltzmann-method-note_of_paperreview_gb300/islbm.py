@@ -94,6 +94,7 @@ def load():
         "islbm_check_finite": [vp, ctypes.POINTER(ctypes.c_longlong)],
         "islbm_destroy": [vp],
         "islbm_diagnostics": [vp, dp],
+        "islbm_diagnostics_noalloc": [vp, dp],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
