@@ -64,8 +64,7 @@ typedef enum islbm_layout {
 typedef enum islbm_kernel {
     ISLBM_KERNEL_AUTO = 0,       /* tiled kernel when the grid allows it, else gather kernel */
     ISLBM_KERNEL_GATHER = 1,     /* one thread per node, stencils read through L1/L2 */
-    ISLBM_KERNEL_TILED = 2,      /* z-marching x-y tiles staged in shared memory */
-    ISLBM_KERNEL_PAIR = 3        /* the tiled kernel with two threads per node (directions split) */
+    ISLBM_KERNEL_TILED = 2       /* z-marching x-y tiles staged in shared memory */
 } islbm_kernel;
 
 /* Parameter set of C/variables.h (same names where the reference has one). */

@@ -316,8 +316,7 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     h->cur = 0;
     h->steps = 0;
     h->use_tiled = false;
-    h->use_pair = false;
-    if (p.kernel == ISLBM_KERNEL_TILED || p.kernel == ISLBM_KERNEL_PAIR || p.kernel == ISLBM_KERNEL_AUTO) {
+    if (p.kernel == ISLBM_KERNEL_TILED || p.kernel == ISLBM_KERNEL_AUTO) {
         h->use_tiled = tiled_supported(k, p.precision);
         if (h->use_tiled) {
             int sms = 0;
@@ -330,10 +329,6 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
             if (make_tiled_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) != 0) h->use_tiled = false;
         }
         if (p.kernel == ISLBM_KERNEL_TILED && !h->use_tiled) { g_last = "tiled kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
-        if (p.kernel == ISLBM_KERNEL_PAIR) {
-            h->use_pair = h->use_tiled && pair_supported(k, p.precision);
-            if (!h->use_pair) { g_last = "paired kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
-        }
     }
     CK(cudaDeviceSynchronize());
     return ISLBM_OK;
@@ -408,7 +403,7 @@ int islbm_step(islbm_handle *h, int nsteps) {
         L.mass = h->p.mass_interval > 0 && (n % (unsigned long long)h->p.mass_interval) == 0ULL;
         L.macros_on = (s == nsteps - 1);
         for (int m = 0; m < 4; m++) L.macros[m] = h->macros[m];
-        cudaError_t e = h->use_pair ? launch_step_pair(L) : (h->use_tiled ? launch_step_tiled(L) : launch_step_gather(L));
+        cudaError_t e = h->use_tiled ? launch_step_tiled(L) : launch_step_gather(L);
         if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
         h->cur = 1 - h->cur;
         h->steps = n;

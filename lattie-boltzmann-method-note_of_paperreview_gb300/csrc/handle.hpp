@@ -29,7 +29,6 @@ struct islbm_handle {
     int cur = 0;
     unsigned long long steps = 0;
     bool use_tiled = false;
-    bool use_pair = false;     // the two-threads-per-node form of the tiled kernel
     TiledConst tiled{};
 };
 

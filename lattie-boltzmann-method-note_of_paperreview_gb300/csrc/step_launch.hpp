@@ -25,7 +25,5 @@ struct StepLaunch {
 cudaError_t launch_step_gather(const StepLaunch &L);
 cudaError_t launch_step_tiled(const StepLaunch &L);
 bool tiled_supported(const StepConst &k, int precision);
-cudaError_t launch_step_pair(const StepLaunch &L);
-bool pair_supported(const StepConst &k, int precision);
 
 }  // namespace islbm

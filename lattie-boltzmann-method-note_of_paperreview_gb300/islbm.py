@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libislbm_gb300.so")
 FP64, FP32, FP16_DEV, BF16_DEV = 0, 1, 2, 3
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16": FP16_DEV, "bf16": BF16_DEV}
 LAYOUT_UNIQUE, LAYOUT_REFERENCE = 0, 1
-KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILED, KERNEL_PAIR = 0, 1, 2, 3
+KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILED = 0, 1, 2
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "HBM budget exceeded",
           5: "non-finite state", 6: "not supported", 7: "no CUDA device"}

@@ -194,21 +194,3 @@ def test_tiled_wide_grid_vs_oracle(islbm_lib, oracle_mod):
     assert rel_l2(g["rho"], r["rho"]) <= 1e-5
     assert rel_l2(velocity(g), velocity(r)) <= 1e-4
 
-
-@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
-@pytest.mark.parametrize("nx,les", [(32, 0.0), (64, 0.1), (128, 0.0)])
-def test_pair_matches_tiled(islbm_lib, prec, nx, les):
-    """The two-threads-per-node kernel does the tiled kernel's arithmetic in the same order:
-    identical populations until the first controller update (the column partial sums of the
-    bulk velocity are grouped differently), then equal to rounding."""
-    nz = 3 * nx // 2 if nx < 128 else 24
-    ny = 2 * nx if nx < 128 else 32
-    re = re_for_tau(0.6, nz)
-    kw = dict(NX=nx, NY=ny, NZ=nz, NDTFRC=20, precision=prec, Re=re, les_cs=les)
-    a = solve(islbm_lib, 19, kernel=2, **kw)
-    b = solve(islbm_lib, 19, kernel=3, **kw)
-    np.testing.assert_array_equal(b["f"], a["f"])
-    a = solve(islbm_lib, 70, kernel=2, mass_interval=9, **kw)
-    b = solve(islbm_lib, 70, kernel=3, mass_interval=9, **kw)
-    assert rel_l2(b["f"], a["f"]) <= 1e-6
-    assert abs(b["force"] - a["force"]) <= 1e-6 * abs(a["force"])
