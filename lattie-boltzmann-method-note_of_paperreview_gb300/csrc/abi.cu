@@ -4,6 +4,7 @@
 // the tables for the unique-node device layout, uploads them with the initial state; the
 // step loop then runs one fused kernel per lattice step on the handle's stream. All device
 // memory is owned by the handle; errors come back as islbm_status codes.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -23,6 +24,8 @@ using namespace islbm;
 namespace {
 
 thread_local std::string g_last;
+
+template <class T> struct Tag { using type = T; };
 
 int cuda_fail(cudaError_t e, const char *what) {
     g_last = std::string(what) + ": " + cudaGetErrorString(e);
@@ -166,6 +169,73 @@ void initial_node(const islbm_handle *h, int x, int y, int z, double *rho, doubl
     }
 }
 
+// Device form of initial_node for every unique node: the same FP64 operations in the same
+// order, each rounded on its own (no contraction), so the state equals the host computation
+// bit for bit; then stored in the storage format as to_storage does.
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+template <class S> __device__ __forceinline__ S to_s(double f, double wq);
+template <> __device__ __forceinline__ double to_s<double>(double f, double) { return f; }
+template <> __device__ __forceinline__ float to_s<float>(double f, double) { return __double2float_rn(f); }
+template <> __device__ __forceinline__ __half to_s<__half>(double f, double wq) { return __float2half_rn(__double2float_rn(ds(f, wq))); }
+template <> __device__ __forceinline__ __nv_bfloat16 to_s<__nv_bfloat16>(double f, double wq) {
+    return __float2bfloat16_rn(__double2float_rn(ds(f, wq)));
+}
+
+template <class S, class C>
+__global__ void init_state_kernel(S *f, C *rho, C *u, C *v, C *w, size_t N, unsigned long long seed, int mode, double ub,
+                                  double amp) {
+    const double W[3] = {1.0/3.0, 1.0/18.0, 1.0/36.0};
+    const signed char E[19][3] = {{0,0,0},{1,0,0},{-1,0,0},{0,1,0},{0,-1,0},{0,0,1},{0,0,-1},{1,1,0},{-1,1,0},{1,-1,0},
+                                  {-1,-1,0},{1,0,1},{-1,0,1},{1,0,-1},{-1,0,-1},{0,1,1},{0,-1,1},{0,1,-1},{0,-1,-1}};
+    for (size_t i = blockIdx.x*(size_t)blockDim.x + threadIdx.x; i < N; i += (size_t)gridDim.x*blockDim.x) {
+        double rr = 1.0, uu = 0.0, vv = 0.0, ww = 0.0;
+        if (mode == 1) {
+            double r3[3];
+            for (int c = 0; c < 3; c++) {
+                unsigned long long s = seed + 0x9E3779B97F4A7C15ULL*(3ULL*i + (unsigned long long)c + 1ULL);
+                s = (s ^ (s >> 30))*0xBF58476D1CE4E5B9ULL;
+                s = (s ^ (s >> 27))*0x94D049BB133111EBULL;
+                s = s ^ (s >> 31);
+                r3[c] = ds(dm(dm((double)(s >> 11), 1.0/9007199254740992.0), 2.0), 1.0);
+            }
+            const double ua = dm(ub, amp);
+            uu = dm(ua, r3[0]);
+            vv = da(ub, dm(ua, r3[1]));
+            ww = dm(ua, r3[2]);
+        }
+        rho[i] = (C)rr; u[i] = (C)uu; v[i] = (C)vv; w[i] = (C)ww;
+        const double udot = da(da(dm(uu, uu), dm(vv, vv)), dm(ww, ww));
+        f[i] = to_s<S>(dm(dm(W[0], rr), ds(1.0, dm(1.5, udot))), W[0]);
+        for (int q = 1; q < 19; q++) {
+            const double eu = da(da(dm((double)E[q][0], uu), dm((double)E[q][1], vv)), dm((double)E[q][2], ww));
+            const double wq = W[q < 7 ? 1 : 2];
+            const double fq = dm(dm(wq, rr), ds(da(da(1.0, dm(3.0, eu)), dm(dm(4.5, eu), eu)), dm(1.5, udot)));
+            f[(size_t)q*N + i] = to_s<S>(fq, wq);
+        }
+    }
+}
+
+cudaError_t launch_init_state(const islbm_handle *h, void *f) {
+    const unsigned grid = (unsigned)std::min<size_t>(4096, (h->N + 255)/256);
+    const auto &p = h->p;
+    auto go = [&](auto s_tag, auto c_tag) {
+        using S = typename decltype(s_tag)::type;
+        using C = typename decltype(c_tag)::type;
+        init_state_kernel<S, C><<<grid, 256, 0, h->stream>>>((S *)f, (C *)h->macros[0], (C *)h->macros[1],
+                                                              (C *)h->macros[2], (C *)h->macros[3], h->N, p.seed,
+                                                              p.init_mode, p.Uref, p.perturb);
+        return cudaGetLastError();
+    };
+    switch (p.precision) {
+    case ISLBM_FP64: return go(Tag<double>{}, Tag<double>{});
+    case ISLBM_FP32: return go(Tag<float>{}, Tag<float>{});
+    case ISLBM_FP16_DEV: return go(Tag<__half>{}, Tag<float>{});
+    default: return go(Tag<__nv_bfloat16>{}, Tag<float>{});
+    }
+}
+
 // host <-> storage conversion of one population array
 void to_storage(int precision, int q, const double *src, void *dst, size_t n) {
     const double wq = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
@@ -264,30 +334,8 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     else pack_tables<float>(h->g, p, blob, h->tf, (char *)h->tabmem);
     CK(cudaMemcpyAsync(h->tabmem, blob.data(), blob.size(), cudaMemcpyHostToDevice, h->stream));
 
-    // initial state on the unique nodes
-    const size_t N = h->N;
-    std::vector<double> f19(19*N), mac(4*N);
-    for (int z = 0; z < p.NZ; z++)
-        for (int y = 0; y < p.NY; y++)
-            for (int x = 0; x < p.NX; x++) {
-                const size_t i = uidx(h, x, y, z);
-                double f[19];
-                initial_node(h, x, y, z, &mac[i], &mac[N + i], &mac[2*N + i], &mac[3*N + i], f);
-                for (int q = 0; q < 19; q++) f19[(size_t)q*N + i] = f[q];
-            }
-    std::vector<char> stage(19*N*h->elem);
-    for (int q = 0; q < 19; q++) to_storage(p.precision, q, &f19[(size_t)q*N], stage.data() + (size_t)q*N*h->elem, N);
-    CK(cudaMemcpyAsync(h->fbuf[0], stage.data(), stage.size(), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    for (int m = 0; m < 4; m++) {
-        if (h->celem == 8) {
-            CK(cudaMemcpy(h->macros[m], &mac[(size_t)m*N], N*8, cudaMemcpyHostToDevice));
-        } else {
-            std::vector<float> fm(N);
-            for (size_t i = 0; i < N; i++) fm[i] = (float)mac[(size_t)m*N + i];
-            CK(cudaMemcpy(h->macros[m], fm.data(), N*4, cudaMemcpyHostToDevice));
-        }
-    }
+    // initial state on the unique nodes, computed on the device
+    CK(launch_init_state(h, h->fbuf[0]));
 
     // step constants and controller
     StepConst &k = h->k;
@@ -310,9 +358,13 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     dxv = dxh.data(); dzv = dzh.data();
     double s0 = 0.0;
     for (int z = 0; z < p.NZ; z++)
-        for (int x = 0; x < p.NX; x++) s0 += mac[2*N + uidx(h, x, k.yplane, z)]*dxv[x]*dzv[z];
+        for (int x = 0; x < p.NX; x++) {
+            double r, u, v, w, f[19];
+            initial_node(h, x, k.yplane, z, &r, &u, &v, &w, f);
+            s0 += v*dxv[x]*dzv[z];
+        }
     c.ub_slot[0] = s0;
-    CK(cudaMemcpy(h->ctrl, &c, sizeof(c), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(h->ctrl, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
     h->cur = 0;
     h->steps = 0;
     h->use_tiled = false;
@@ -330,7 +382,7 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
         }
         if (p.kernel == ISLBM_KERNEL_TILED && !h->use_tiled) { g_last = "tiled kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
     }
-    CK(cudaDeviceSynchronize());
+    CK(cudaStreamSynchronize(h->stream));
     return ISLBM_OK;
 }
 

@@ -199,10 +199,12 @@ void retire(islbm_server *s, Solve *v, int status) {
     s->used -= v->bytes;
 }
 
-int admit(islbm_server *s) {
+// Admit queued requests in arrival order while the budget allows; the new solves are appended
+// to `fresh` (they join the active set when the caller says so).
+int admit(islbm_server *s, std::vector<Solve *> &fresh) {
     while (!s->queue.empty()) {
         Solve *v = s->queue.front();
-        if (s->used + v->bytes > s->budget && !s->active.empty()) break;   // wait for memory
+        if (s->used + v->bytes > s->budget && !(s->active.empty() && fresh.empty())) break;   // wait for memory
         if (s->used + v->bytes > s->budget) {   // can never fit
             s->queue.pop_front();
             v->status = ISLBM_SOLVE_REJECTED;
@@ -225,7 +227,7 @@ int admit(islbm_server *s) {
         v->status = ISLBM_SOLVE_ACTIVE;
         v->t_admit = now_s() - s->t0;
         s->used += v->bytes;
-        s->active.push_back(v);
+        fresh.push_back(v);
     }
     return ISLBM_OK;
 }
@@ -389,8 +391,14 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
     if (!s) return ISLBM_ERR_INVALID_ARGUMENT;
     const double t_start = now_s();
     SK(cudaSetDevice(s->device));
-    int st = admit(s);
-    if (st != ISLBM_OK) return st;
+    std::vector<Solve *> fresh;
+    int st = ISLBM_OK;
+    if (s->active.empty()) {   // nothing on the device: admit now
+        st = admit(s, fresh);
+        if (st != ISLBM_OK) return st;
+        s->active.swap(fresh);
+        fresh.clear();
+    }
     if (!s->active.empty()) {
         // chunk length: up to the next convergence check / step cap of any active solve
         int steps = s->chunk;
@@ -420,6 +428,10 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             v->steps += steps;
             s->updates += (long long)steps*(long long)v->h->N;
         }
+        // while the chunk runs: set up the requests that arrived (host precompute, uploads on
+        // their own streams); they join the active set after this chunk
+        st = admit(s, fresh);
+        if (st != ISLBM_OK) return st;
         for (Solve *v : singles) {
             st = islbm_sync(v->h);
             if (st != ISLBM_OK) return st;
@@ -453,8 +465,7 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             else keep.push_back(v);
         }
         s->active.swap(keep);
-        st = admit(s);
-        if (st != ISLBM_OK) return st;
+        for (Solve *v : fresh) s->active.push_back(v);
     }
     s->busy += now_s() - t_start;
     if (n_active) *n_active = (int)s->active.size();

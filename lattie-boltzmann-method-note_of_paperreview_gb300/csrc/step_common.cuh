@@ -95,9 +95,18 @@ struct StepConst {
 enum { XI3 = 0, XI4, XI5, XI6, XI15, XI16, XI17, XI18 };
 enum { B_XB37 = 0, B_XB38, B_YB378, B_XIB378, B_XB49, B_XB410, B_YB4910, B_XIB4910, B_YB15, B_XIB15, B_YB16, B_XIB16 };
 
+// Square root and reciprocal of the collision: IEEE in FP64 (the parity path); in FP32 the
+// hardware approximations (a few ulp, no special-value branches), well inside the FP32
+// tolerance of the step.
 template <class C> __device__ __forceinline__ C my_sqrt(C v);
 template <> __device__ __forceinline__ double my_sqrt<double>(double v) { return sqrt(v); }
-template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return sqrtf(v); }
+template <> __device__ __forceinline__ float my_sqrt<float>(float v) { return v > 0.f ? v*rsqrtf(v) : 0.f; }
+template <class C> __device__ __forceinline__ C my_rcp(C v);
+template <> __device__ __forceinline__ double my_rcp<double>(double v) { return 1.0/v; }
+template <> __device__ __forceinline__ float my_rcp<float>(float v) { return __fdividef(1.f, v); }
+template <class C> __device__ __forceinline__ C my_div(C a, C b);
+template <> __device__ __forceinline__ double my_div<double>(double a, double b) { return a/b; }
+template <> __device__ __forceinline__ float my_div<float>(float a, float b) { return __fdividef(a, b); }
 
 // Collision tail of C/evolution.h:597-652 for one node: mass correction, moments,
 // equilibrium, MRT relaxation (optionally with the Smagorinsky rate) and body force.
@@ -110,7 +119,7 @@ __device__ __forceinline__ void collide_node(C (&F)[19], C rho_modify, C f6, C f
 #pragma unroll
     for (int q = 1; q < 19; q++) r = r + F[q];
     rho_s = r;
-    const C inv = C(1)/r;
+    const C inv = my_rcp<C>(r);
     u1 = (F[1] + F[7] + F[9] + F[11] + F[13] - (F[2] + F[8] + F[10] + F[12] + F[14]))*inv;
     v1 = (F[3] + F[7] + F[8] + F[15] + F[17] - (F[4] + F[9] + F[10] + F[16] + F[18]))*inv;
     w1 = (F[5] + F[11] + F[12] + F[15] + F[16] - (F[6] + F[13] + F[14] + F[17] + F[18]))*inv;
@@ -132,12 +141,12 @@ __device__ __forceinline__ void collide_node(C (&F)[19], C rho_modify, C f6, C f
             d[qm[m]] = F[qm[m]] - a*(sym - asym);
         }
     }
-    C s_nu = C(1)/tau;
+    C s_nu = my_rcp<C>(tau);
     if constexpr (LES) {
         const C Qn = pi_neq_norm2(d);
         const C nu0 = (tau - C(0.5))*C(1.0/3.0);
-        const C S = (my_sqrt<C>(nu0*nu0 + C(18)*lesC*my_sqrt<C>(Qn)) - nu0)/(C(6)*lesC);
-        s_nu = C(1)/(tau + C(3)*lesC*S);
+        const C S = my_div<C>(my_sqrt<C>(nu0*nu0 + C(18)*lesC*my_sqrt<C>(Qn)) - nu0, C(6)*lesC);
+        s_nu = my_rcp<C>(tau + C(3)*lesC*S);
     }
     mrt_relax<C>(F, d, C(1.19), C(1.4), C(1.2), s_nu, C(1.4), C(1.5));
     F[3] += f6; F[4] -= f6;

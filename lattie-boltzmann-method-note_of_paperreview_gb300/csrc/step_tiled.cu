@@ -68,7 +68,8 @@ struct Lay {
     static constexpr int ybuf_off = NSTAGES*stage_bytes;
     static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
     static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
-    static constexpr int smem_bytes = bar_off + NSTAGES*8;
+    static constexpr int flag_off = bar_off + NSTAGES*8;   // CTA-wide "a wait timed out" flag
+    static constexpr int smem_bytes = flag_off + 16;
 };
 
 // Filtered values of one plane for the node of this thread (pairs of directions).
@@ -213,18 +214,20 @@ struct TiledKernel {
         F[1] = a; F[2] = b;
     }
 
-    // Issued by warp 0: lane 0 posts the expected bytes, then lane q copies population q
-    // (two pieces when the halo wraps) and lanes 19, 20 the target data.
-    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, int lane) const {
+    // Copy job q of a plane (1..18: population q, two pieces when the halo wraps; 19, 20: the
+    // target's xi weights and f0 row). Jobs are spread over the four warps (job q on warp q & 3,
+    // lane q >> 2) so that no warp serialises all the copy issues; thread 0 posts the expected
+    // bytes (a copy may complete before that: the phase cannot end while the arrival is due).
+    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, int tid) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int NY = k.NY, NZ = k.NZ;
         const size_t N = (size_t)NX*NY*NZ;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
         const bool tgt = p >= 7 && p <= NZ - 1;
-        if (lane == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
-        __syncwarp();
+        if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         S *pops = (S *)stage;
-        const int q = lane;
+        const int lane = tid & 31;
+        const int q = lane < 6 ? 4*lane + (tid >> 5) : 0;
         if (q >= 1 && q < 19) {
             S *dst = pops + LY::off(q);
             const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
@@ -238,11 +241,11 @@ struct TiledKernel {
                 if (first < rows) bulk_g2s(dst + (size_t)first*NX, plane_base, (rows - first)*row_bytes, bar);
             }
         }
-        if (tgt && lane == 19) {
+        if (tgt && q == 19) {
             const int z = p - 3;
             bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)z*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
         }
-        if (tgt && lane == 20) {
+        if (tgt && q == 20) {
             const int z = p - 3;
             bulk_g2s(stage + LY::f0_off, fo + ((size_t)z*NY + y0)*NX, TY*row_bytes, bar);
         }
@@ -269,14 +272,15 @@ struct TiledKernel {
         int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
 
-    // Warp 0: start the copies of plane p into stage s and record them as pending. After a
-    // timed-out wait in any lane of warp 0 no new copy is started.
-    __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity,
-                                          bool faulted) const {
-        if (__any_sync(0xffffffffu, faulted)) return;
+    // Every thread, after a CTA barrier: start the copies of plane p into stage s; warp 0
+    // records them as pending. After a timed-out wait anywhere in the CTA (the shared flag,
+    // written before the barrier) no thread starts a copy.
+    __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity) const {
+        if (*(volatile int *)(smem + LY::flag_off)) return;
         fence_proxy_async();
         issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, y0, L.tid);
-        parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
+        if (L.tid < 32)
+            parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
     }
 
     // One source plane: wait for its copies, filter, return the plane's slot values.
@@ -290,6 +294,7 @@ struct TiledKernel {
         unsigned char *stage = smem + (size_t)s*LY::stage_bytes;
         const S *raw = (const S *)stage;
         if (mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted)) parity &= ~(1u << (PEND + s));
+        else if (faulted) *(volatile int *)(smem + LY::flag_off) = 1;
         parity ^= 1u << s;
         Slot v;
         {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
@@ -314,7 +319,7 @@ struct TiledKernel {
         }
         __syncthreads();
         // every thread has finished plane i-1: its stage can take plane i + NSTAGES - 1
-        if (L.tid < 32 && p + NSTAGES - 1 <= p1) issue(smem, (i + NSTAGES - 1) % NSTAGES, p + NSTAGES - 1, y0, L, parity, faulted);
+        if (p + NSTAGES - 1 <= p1) issue(smem, (i + NSTAGES - 1) % NSTAGES, p + NSTAGES - 1, y0, L, parity);
         {   // spanwise filter: two nodes of one row, five directions of one departure side
             const int m = NX - 1;
             const int x0 = L.xx0;
@@ -405,8 +410,7 @@ struct TiledKernel {
         const int y0 = tile*TY;
         const int p1 = NZ - 1;
         __syncthreads();   // every thread is done with every stage of the previous column
-        if (L.tid < 32)
-            for (int s = 0; s < NSTAGES - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity, faulted);
+        for (int s = 0; s < NSTAGES - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity);
         const int y = y0 + L.yl;
         // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
 #pragma unroll 1
@@ -440,6 +444,7 @@ struct TiledKernel {
         const Lane L = lane();
         if (L.tid == 0) {
             for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
+            *(volatile int *)(smem + LY::flag_off) = 0;
             fence_mbar_init();
         }
         __syncthreads();
@@ -492,6 +497,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
     const int tid = threadIdx.x;
     if (tid == 0) {
         for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
+        *(volatile int *)(smem + LY::flag_off) = 0;
         fence_mbar_init();
     }
     unsigned parity = 0;
