@@ -156,6 +156,42 @@ ISLBM_API int islbm_diagnostics(islbm_handle *h, double *out);
  * scratch and race: run them one at a time. */
 ISLBM_API int islbm_diagnostics_noalloc(islbm_handle *h, double *out);
 
+/* Time-averaged statistics (MeanVars of C/statistics.h:122-174, enabled there by TBSWITCH,
+ * C/variables.h:32): per-node FP64 sums of the quantities below over samples of the current
+ * macroscopic fields, with P = rho/3 - 1/3 and KT = (u^2 + v^2 + w^2)/2. Call
+ * islbm_stats_accumulate after islbm_step (which leaves the fields of its last step); the first
+ * call allocates ISLBM_STAT_COUNT*N doubles on the device. The reference's velocity-gradient
+ * statistics (MeanDerivatives, C/statistics.h:176-222) are not provided: their wall-normal
+ * weights (ZSlopePara) are never set in the reference. */
+typedef enum islbm_stat {
+    ISLBM_STAT_U = 0, ISLBM_STAT_V, ISLBM_STAT_W, ISLBM_STAT_P,
+    ISLBM_STAT_UU, ISLBM_STAT_UV, ISLBM_STAT_UW, ISLBM_STAT_VV, ISLBM_STAT_VW, ISLBM_STAT_WW,
+    ISLBM_STAT_PU, ISLBM_STAT_PV, ISLBM_STAT_PW, ISLBM_STAT_PP, ISLBM_STAT_KT,
+    ISLBM_STAT_UUU, ISLBM_STAT_UUV, ISLBM_STAT_UUW, ISLBM_STAT_VVU, ISLBM_STAT_VVV, ISLBM_STAT_VVW,
+    ISLBM_STAT_WWU, ISLBM_STAT_WWV, ISLBM_STAT_WWW,
+    ISLBM_STAT_COUNT
+} islbm_stat;
+/* zero the sums (allocating them on first use) */
+ISLBM_API int islbm_stats_reset(islbm_handle *h);
+/* add one sample (the fields of the last step); asynchronous on the handle's stream */
+ISLBM_API int islbm_stats_accumulate(islbm_handle *h);
+ISLBM_API int islbm_stats_samples(islbm_handle *h, long long *samples);
+/* time mean (sum / samples) of one quantity, unique or reference layout (the reference writes
+ * these fields with OutputData, C/fileIO.h:52-67) */
+ISLBM_API int islbm_stats_mean(islbm_handle *h, int quantity, double *out, int layout);
+/* spanwise average of the time mean at streamwise row y (0 <= y < NY): NZ values, wall-normal
+ * index 0 at the hill surface (the profiles of C/fileIO.h:118-249) */
+ISLBM_API int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *out);
+
+/* Checkpoint / restart in the reference's files (OutputData / InitialUsingBkpData,
+ * C/fileIO.h:52-67, 262-266, 298-354): <dir>/{rho,u,v,w,f0..f18}_<rank>.bin as raw FP64 arrays
+ * of NX6*NZ6*NYD6 values in the padded layout, and the body force as text in <dir>/0_force.dat.
+ * The controller state (force, bulk-velocity window, step counter) is also written to
+ * <dir>/islbm_ctrl_<rank>.bin; read uses it when present (exact resume) and otherwise the text
+ * force, as the reference does. The directory must exist. */
+ISLBM_API int islbm_checkpoint_write(islbm_handle *h, const char *dir, int rank);
+ISLBM_API int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank);
+
 ISLBM_API int islbm_destroy(islbm_handle *h);
 
 ISLBM_API const char *islbm_status_string(int status);

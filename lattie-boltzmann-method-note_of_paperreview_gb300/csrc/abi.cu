@@ -303,6 +303,7 @@ void free_handle_impl(islbm_handle *h) {
     for (int m = 0; m < 4; m++) if (h->macros[m]) cudaFree(h->macros[m]);
     if (h->tabmem) cudaFree(h->tabmem);
     if (h->ctrl) cudaFree(h->ctrl);
+    if (h->stats) cudaFree(h->stats);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -392,6 +393,8 @@ namespace islbm {
 int handle_init(const islbm_params *p, islbm_handle *h) { return init_impl(p, h); }
 void handle_free(islbm_handle *h) { free_handle_impl(h); }
 int report_cuda(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+void unique_to_reference_layout(const islbm_handle *h, const double *u, double *r) { unique_to_reference(h, u, r); }
+void reference_to_unique_layout(const islbm_handle *h, const double *r, double *u) { reference_to_unique(h, r, u); }
 int report_status(int status, const char *msg) {
     g_last = msg;
     return status;

@@ -29,6 +29,8 @@ struct islbm_handle {
     int cur = 0;
     unsigned long long steps = 0;
     bool use_tiled = false;
+    double *stats = nullptr;   // time-average accumulators, ISLBM_STAT_COUNT x N (allocated on first use)
+    long long stats_samples = 0;
     TiledConst tiled{};
 };
 
@@ -41,4 +43,8 @@ void handle_free(islbm_handle *h);
 int report_cuda(cudaError_t e, const char *what);
 // record a message for islbm_status_string and return `status`
 int report_status(int status, const char *msg);
+// unique [z][y][x] field -> the reference's padded layout (NYD6, NZ6, NX6)
+void unique_to_reference_layout(const islbm_handle *h, const double *u, double *r);
+// the reference's padded layout -> unique [z][y][x] (interior nodes)
+void reference_to_unique_layout(const islbm_handle *h, const double *r, double *u);
 }

@@ -1,0 +1,132 @@
+// Time-averaged turbulence statistics of a solve (MeanVars, C/statistics.h:122-174).
+//
+// Per unique node, FP64 sums over samples of the 24 quantities of the reference, in its order:
+//   U V W P, UU UV UW VV VW WW, PU PV PW PP, KT, UUU UUV UUW VVU VVV VVW WWU WWV WWW
+// with P = rho/3 - 1/3 and KT = (u^2 + v^2 + w^2)/2, taken from the macroscopic fields of the
+// last step (islbm_step writes them on its last step). The accumulators are one allocation of
+// 24*N doubles, laid out [quantity][z][y][x]; a sample reads 16 B (FP32 fields) or 32 B (FP64)
+// and updates 24 x 8 B per node, so it is HBM bound at about 400 B per node.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "handle.hpp"
+
+namespace islbm {
+namespace {
+
+template <class C>
+__global__ void stats_kernel(const C *__restrict__ rho, const C *__restrict__ u, const C *__restrict__ v,
+                             const C *__restrict__ w, double *__restrict__ acc, size_t n) {
+    for (size_t i = blockIdx.x*(size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x*blockDim.x) {
+        const double u1 = (double)u[i], v1 = (double)v[i], w1 = (double)w[i];
+        const double p1 = 1.0/3.0*(double)rho[i] - 1.0/3.0;
+        double *a = acc + i;
+        // same products as the reference accumulates (C/statistics.h:145-172)
+        a[0*n] += u1; a[1*n] += v1; a[2*n] += w1; a[3*n] += p1;
+        a[4*n] += u1*u1; a[5*n] += u1*v1; a[6*n] += u1*w1; a[7*n] += v1*v1; a[8*n] += v1*w1; a[9*n] += w1*w1;
+        a[10*n] += p1*u1; a[11*n] += p1*v1; a[12*n] += p1*w1; a[13*n] += p1*p1;
+        a[14*n] += 0.5*(u1*u1 + v1*v1 + w1*w1);
+        a[15*n] += u1*u1*u1; a[16*n] += u1*u1*v1; a[17*n] += u1*u1*w1;
+        a[18*n] += v1*v1*u1; a[19*n] += v1*v1*v1; a[20*n] += v1*v1*w1;
+        a[21*n] += w1*w1*u1; a[22*n] += w1*w1*v1; a[23*n] += w1*w1*w1;
+    }
+}
+
+}  // namespace
+}  // namespace islbm
+
+using namespace islbm;
+
+extern "C" {
+
+int islbm_stats_reset(islbm_handle *h) {
+    if (!h) return ISLBM_ERR_INVALID_ARGUMENT;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    const size_t bytes = (size_t)ISLBM_STAT_COUNT*h->N*sizeof(double);
+    if (!h->stats) {
+        e = cudaMalloc(&h->stats, bytes);
+        if (e != cudaSuccess) { h->stats = nullptr; return report_cuda(e, "cudaMalloc(statistics)"); }
+    }
+    e = cudaMemsetAsync(h->stats, 0, bytes, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return report_cuda(e, "statistics reset");
+    h->stats_samples = 0;
+    return ISLBM_OK;
+}
+
+int islbm_stats_accumulate(islbm_handle *h) {
+    if (!h) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->stats) {
+        const int st = islbm_stats_reset(h);
+        if (st != ISLBM_OK) return st;
+    }
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaDeviceGetAttribute");
+    const unsigned grid = (unsigned)std::min<size_t>((size_t)sms*8, (h->N + 255)/256);
+    if (h->celem == 8)
+        stats_kernel<double><<<grid, 256, 0, h->stream>>>((const double *)h->macros[0], (const double *)h->macros[1],
+                                                          (const double *)h->macros[2], (const double *)h->macros[3],
+                                                          h->stats, h->N);
+    else
+        stats_kernel<float><<<grid, 256, 0, h->stream>>>((const float *)h->macros[0], (const float *)h->macros[1],
+                                                         (const float *)h->macros[2], (const float *)h->macros[3],
+                                                         h->stats, h->N);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return report_cuda(e, "statistics kernel launch");
+    h->stats_samples++;
+    return ISLBM_OK;
+}
+
+int islbm_stats_samples(islbm_handle *h, long long *samples) {
+    if (!h || !samples) return ISLBM_ERR_INVALID_ARGUMENT;
+    *samples = h->stats_samples;
+    return ISLBM_OK;
+}
+
+int islbm_stats_mean(islbm_handle *h, int quantity, double *out, int layout) {
+    if (!h || !out || quantity < 0 || quantity >= ISLBM_STAT_COUNT || layout < 0 || layout > 1)
+        return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->stats || h->stats_samples == 0) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics samples");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    std::vector<double> sum(h->N);
+    e = cudaMemcpyAsync(sum.data(), h->stats + (size_t)quantity*h->N, h->N*sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return report_cuda(e, "statistics read");
+    const double inv = 1.0/(double)h->stats_samples;
+    for (size_t i = 0; i < h->N; i++) sum[i] *= inv;
+    if (layout == ISLBM_LAYOUT_REFERENCE) unique_to_reference_layout(h, sum.data(), out);
+    else std::memcpy(out, sum.data(), h->N*sizeof(double));
+    return ISLBM_OK;
+}
+
+int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *out) {
+    if (!h || !out || quantity < 0 || quantity >= ISLBM_STAT_COUNT || y < 0 || y >= h->p.NY)
+        return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->stats || h->stats_samples == 0) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics samples");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    const int NX = h->p.NX, NY = h->p.NY, NZ = h->p.NZ;
+    std::vector<double> slab((size_t)NX*NZ);
+    // the (z, x) slab of streamwise row y: NZ rows of NX values, NY*NX apart
+    e = cudaMemcpy2DAsync(slab.data(), NX*sizeof(double), h->stats + (size_t)quantity*h->N + (size_t)y*NX,
+                          (size_t)NY*NX*sizeof(double), NX*sizeof(double), NZ, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return report_cuda(e, "statistics profile read");
+    const double inv = 1.0/((double)h->stats_samples*NX);
+    for (int z = 0; z < NZ; z++) {
+        double s = 0.0;
+        for (int x = 0; x < NX; x++) s += slab[(size_t)z*NX + x];
+        out[z] = s*inv;
+    }
+    return ISLBM_OK;
+}
+
+}  // extern "C"

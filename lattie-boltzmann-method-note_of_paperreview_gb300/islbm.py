@@ -62,6 +62,10 @@ class SolveInfo(ctypes.Structure):
                 ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_done", ctypes.c_double)]
 
 
+# time-averaged quantities of islbm_stats_* (islbm_stat order)
+STATS = ["U", "V", "W", "P", "UU", "UV", "UW", "VV", "VW", "WW", "PU", "PV", "PW", "PP", "KT",
+         "UUU", "UUV", "UUW", "VVU", "VVV", "VVW", "WWU", "WWV", "WWW"]
+
 SOLVE_STATUS = {0: "queued", 1: "active", 2: "converged", 3: "capped", 4: "diverged", 5: "rejected"}
 
 _lib = None
@@ -95,6 +99,13 @@ def load():
         "islbm_destroy": [vp],
         "islbm_diagnostics": [vp, dp],
         "islbm_diagnostics_noalloc": [vp, dp],
+        "islbm_checkpoint_write": [vp, ctypes.c_char_p, ip],
+        "islbm_checkpoint_read": [vp, ctypes.c_char_p, ip],
+        "islbm_stats_reset": [vp],
+        "islbm_stats_accumulate": [vp],
+        "islbm_stats_samples": [vp, ctypes.POINTER(ctypes.c_longlong)],
+        "islbm_stats_mean": [vp, ip, vp, ip],
+        "islbm_stats_profile": [vp, ip, ip, vp],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
@@ -263,6 +274,37 @@ class Solver:
         out = (ctypes.c_double * 4)()
         check(self._L.islbm_diagnostics(self._h, out))
         return {"mass": out[0], "momentum_y": out[1], "kinetic_energy": out[2], "max_speed": out[3]}
+
+    def checkpoint_write(self, directory, rank=0):
+        check(self._L.islbm_checkpoint_write(self._h, os.fsencode(directory), int(rank)))
+
+    def checkpoint_read(self, directory, rank=0):
+        check(self._L.islbm_checkpoint_read(self._h, os.fsencode(directory), int(rank)))
+
+    def stats_reset(self):
+        check(self._L.islbm_stats_reset(self._h))
+
+    def stats_accumulate(self):
+        check(self._L.islbm_stats_accumulate(self._h))
+
+    def stats_samples(self):
+        n = ctypes.c_longlong()
+        check(self._L.islbm_stats_samples(self._h, ctypes.byref(n)))
+        return n.value
+
+    def stats_mean(self, quantity, layout=LAYOUT_UNIQUE):
+        """Time mean of one quantity (name from STATS or index)."""
+        q = STATS.index(quantity) if isinstance(quantity, str) else int(quantity)
+        out = np.zeros(self._shape(layout), dtype=np.float64)
+        check(self._L.islbm_stats_mean(self._h, q, out.ctypes.data_as(ctypes.c_void_p), int(layout)))
+        return out
+
+    def stats_profile(self, quantity, y):
+        """Spanwise-averaged time mean at streamwise row y: NZ values from the hill surface up."""
+        q = STATS.index(quantity) if isinstance(quantity, str) else int(quantity)
+        out = np.zeros(self.params.NZ, dtype=np.float64)
+        check(self._L.islbm_stats_profile(self._h, q, int(y), out.ctypes.data_as(ctypes.c_void_p)))
+        return out
 
     def healthy(self):
         bad = ctypes.c_longlong()

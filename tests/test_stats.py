@@ -1,0 +1,42 @@
+"""Time-averaged statistics (MeanVars, C/statistics.h:122-174) against the same sums taken on the
+host from islbm_fields after each sampled step, for FP64 and FP32 fields."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def host_quantities(f):
+    u, v, w = f["u"], f["v"], f["w"]
+    p = 1.0 / 3.0 * f["rho"] - 1.0 / 3.0
+    return {"U": u, "V": v, "W": w, "P": p, "UU": u * u, "UV": u * v, "UW": u * w, "VV": v * v, "VW": v * w,
+            "WW": w * w, "PU": p * u, "PV": p * v, "PW": p * w, "PP": p * p, "KT": 0.5 * (u * u + v * v + w * w),
+            "UUU": u * u * u, "UUV": u * u * v, "UUW": u * u * w, "VVU": v * v * u, "VVV": v * v * v,
+            "VVW": v * v * w, "WWU": w * w * u, "WWV": w * w * v, "WWW": w * w * w}
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_stats_match_host_sums(islbm_lib, precision):
+    islbm = islbm_lib
+    p = islbm.default_params(NX=32, NY=64, NZ=48, Re=58.9, Uref=0.05, precision=precision, init_mode=1, seed=21)
+    with islbm.Solver(p) as s:
+        acc = None
+        s.stats_reset()
+        for k in range(5):
+            s.step(7)
+            s.stats_accumulate()
+            q = host_quantities(s.fields())
+            acc = q if acc is None else {n: acc[n] + q[n] for n in q}
+        assert s.stats_samples() == 5
+        for i, name in enumerate(islbm.STATS):
+            got = s.stats_mean(name)
+            ref = acc[name] / 5
+            scale = np.abs(ref).max()
+            np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-14 * scale, err_msg=name)
+        prof = s.stats_profile("V", 10)
+        np.testing.assert_allclose(prof, (acc["V"] / 5)[:, 10, :].mean(axis=1), rtol=1e-12)
+        ref_layout = s.stats_mean("U", layout=islbm.LAYOUT_REFERENCE)
+        assert ref_layout.shape == (p.NY + 7, p.NZ + 6, p.NX + 7)
+        np.testing.assert_array_equal(ref_layout[3:-4, 3:-3, 3:-4].transpose(1, 0, 2), s.stats_mean("U"))
+        s.stats_reset()
+        assert s.stats_samples() == 0
