@@ -115,6 +115,8 @@ struct Group {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     std::string key;
+    cudaStream_t stream = nullptr;   // batches run side by side, each on its own stream
+    cudaEvent_t done = nullptr;      // end of this batch's chunk
 };
 
 }  // namespace
@@ -162,10 +164,13 @@ size_t solve_bytes(const islbm_params &p) {
 }
 
 void free_group(Group *g) {
+    if (g->stream) cudaStreamSynchronize(g->stream);
     if (g->graph) cudaGraphExecDestroy(g->graph);
     if (g->descs) cudaFree(g->descs);
     if (g->items) cudaFree(g->items);
-    g->graph = nullptr; g->descs = nullptr; g->items = nullptr;
+    if (g->done) cudaEventDestroy(g->done);
+    if (g->stream) cudaStreamDestroy(g->stream);
+    g->graph = nullptr; g->descs = nullptr; g->items = nullptr; g->done = nullptr; g->stream = nullptr;
 }
 
 // batched launches advance a solve on the device (its controller's step counter picks the
@@ -274,8 +279,10 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
         g->nitems = (int)items.size();
         SK(cudaMalloc(&g->descs, hd.size()));
         SK(cudaMalloc(&g->items, items.size()*sizeof(int2)));
-        SK(cudaMemcpyAsync(g->descs, hd.data(), hd.size(), cudaMemcpyHostToDevice, s->stream));
-        SK(cudaMemcpyAsync(g->items, items.data(), items.size()*sizeof(int2), cudaMemcpyHostToDevice, s->stream));
+        SK(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        SK(cudaEventCreateWithFlags(&g->done, cudaEventDisableTiming));
+        SK(cudaMemcpyAsync(g->descs, hd.data(), hd.size(), cudaMemcpyHostToDevice, g->stream));
+        SK(cudaMemcpyAsync(g->items, items.data(), items.size()*sizeof(int2), cudaMemcpyHostToDevice, g->stream));
         out.push_back(g.get());
         s->groups[kv.first] = std::move(g);
     }
@@ -305,9 +312,9 @@ int tune(islbm_server *s, Group *g) {
     SK(cudaEventCreate(&e1));
     for (int c = 0; c < 3; c++) {
         if (c > 0 && cand[c] == cand[c - 1]) continue;
-        SK(cudaEventRecord(e0, s->stream));
-        SK(launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, cand[c], 1, s->stream));
-        SK(cudaEventRecord(e1, s->stream));
+        SK(cudaEventRecord(e0, g->stream));
+        SK(launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, cand[c], 1, g->stream));
+        SK(cudaEventRecord(e1, g->stream));
         SK(cudaEventSynchronize(e1));
         launched++;
         float ms = 0;
@@ -328,18 +335,18 @@ int run_group_chunk(islbm_server *s, Group *g, int steps) {
         g->graph = nullptr;
         cudaGraph_t graph;
         SK(prepare_step_tiled_batch(g->precision, g->NX, g->les));
-        SK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        SK(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
         for (int j = 0; j < steps; j++) {
             cudaError_t e = launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, g->grid,
-                                                    j == steps - 1, s->stream);
-            if (e != cudaSuccess) { cudaStreamEndCapture(s->stream, &graph); return fail(s, e, "batched step capture"); }
+                                                    j == steps - 1, g->stream);
+            if (e != cudaSuccess) { cudaStreamEndCapture(g->stream, &graph); return fail(s, e, "batched step capture"); }
         }
-        SK(cudaStreamEndCapture(s->stream, &graph));
+        SK(cudaStreamEndCapture(g->stream, &graph));
         SK(cudaGraphInstantiate(&g->graph, graph, 0));
         cudaGraphDestroy(graph);
         g->graph_steps = steps;
     }
-    SK(cudaGraphLaunch(g->graph, s->stream));
+    SK(cudaGraphLaunch(g->graph, g->stream));
     return ISLBM_OK;
 }
 
@@ -427,6 +434,11 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             if (st != ISLBM_OK) return st;
             v->steps += steps;
             s->updates += (long long)steps*(long long)v->h->N;
+        }
+        // the convergence measure (on the server stream) waits for every batch
+        for (Group *g : groups) {
+            SK(cudaEventRecord(g->done, g->stream));
+            SK(cudaStreamWaitEvent(s->stream, g->done, 0));
         }
         // while the chunk runs: set up the requests that arrived (host precompute, uploads on
         // their own streams); they join the active set after this chunk

@@ -115,9 +115,18 @@ template <class C, bool LES>
 __device__ __forceinline__ void collide_node(C (&F)[19], C rho_modify, C f6, C f12, C tau, C lesC,
                                              C &rho_s, C &u1, C &v1, C &w1) {
     F[0] = F[0] + rho_modify;
-    C r = F[0];
+    C r;
+    if constexpr (sizeof(C) == 8) {
+        // FP64: the reference's summation order (C/evolution.h:600-602)
+        r = F[0];
 #pragma unroll
-    for (int q = 1; q < 19; q++) r = r + F[q];
+        for (int q = 1; q < 19; q++) r = r + F[q];
+    } else {
+        // FP32: a balanced tree (depth 5 instead of a chain of 18 dependent adds)
+        const C a0 = F[0] + F[1], a1 = F[2] + F[3], a2 = F[4] + F[5], a3 = F[6] + F[7], a4 = F[8] + F[9];
+        const C a5 = F[10] + F[11], a6 = F[12] + F[13], a7 = F[14] + F[15], a8 = F[16] + F[17];
+        r = (((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7))) + (a8 + F[18]);
+    }
     rho_s = r;
     const C inv = my_rcp<C>(r);
     u1 = (F[1] + F[7] + F[9] + F[11] + F[13] - (F[2] + F[8] + F[10] + F[12] + F[14]))*inv;

@@ -226,8 +226,7 @@ struct TiledKernel {
         const bool tgt = p >= 7 && p <= NZ - 1;
         if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         S *pops = (S *)stage;
-        const int lane = tid & 31;
-        const int q = lane < 6 ? 4*lane + (tid >> 5) : 0;
+        const int q = 4*(tid & 31) + (tid >> 5);   // lanes 0..5 only
         if (q >= 1 && q < 19) {
             S *dst = pops + LY::off(q);
             const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
@@ -251,10 +250,10 @@ struct TiledKernel {
         }
     }
 
-    // Warp 0, at the end of the kernel: bounded wait for copies still pending (only after a
+    // Thread 0, at the end of the kernel: bounded wait for copies still pending (only after a
     // timeout; in a healthy run every copy has been consumed).
     __device__ __forceinline__ void drain(unsigned char *smem, unsigned parity, int tid) const {
-        if (tid >= 32) return;
+        if (tid != 0) return;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         for (int s = 0; s < NSTAGES; s++) {
             if (!((parity >> (PEND + s)) & 1u)) continue;
@@ -272,14 +271,15 @@ struct TiledKernel {
         int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
 
-    // Every thread, after a CTA barrier: start the copies of plane p into stage s; warp 0
-    // records them as pending. After a timed-out wait anywhere in the CTA (the shared flag,
-    // written before the barrier) no thread starts a copy.
+    // After a CTA barrier, lanes 0..5 of every warp start the copies of plane p into stage s;
+    // thread 0 (which posts the expected bytes) records the stage as pending. After a timed-out
+    // wait anywhere in the CTA (the shared flag, written before the barrier) no copy starts.
     __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity) const {
+        if ((L.tid & 31) >= 6) return;
         if (*(volatile int *)(smem + LY::flag_off)) return;
         fence_proxy_async();
         issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, y0, L.tid);
-        if (L.tid < 32)
+        if (L.tid == 0)
             parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
     }
 
