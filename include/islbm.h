@@ -88,6 +88,8 @@ typedef struct islbm_params {
     int device;                /* CUDA device ordinal */
     int kernel;                /* islbm_kernel */
     size_t hbm_budget_bytes;   /* refuse solves above this many device bytes (0 = no limit) */
+    int geometry;              /* 0: periodic hill (HillFunction, C/model.h:4-68); 1: flat channel
+                                  (ChannelFunction, C/model.h:70-73) */
 } islbm_params;
 
 typedef struct islbm_handle islbm_handle;
@@ -191,6 +193,14 @@ ISLBM_API int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *
  * force, as the reference does. The directory must exist. */
 ISLBM_API int islbm_checkpoint_write(islbm_handle *h, const char *dir, int rank);
 ISLBM_API int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank);
+
+/* Result files of the reference from the current fields: the Tecplot ASCII velocity file of
+ * fileIO_velocity (C/fileIO.h:69-87), the Tecplot binary file of Output3Dvelocity
+ * (C/fileIO.h:502-659, velocities / Uref) and one appended Monitor.dat line of Launch_Monitor
+ * (C/monitor.h:4-26: step, v, u, w at the centre node, force). */
+ISLBM_API int islbm_write_tecplot_ascii(islbm_handle *h, const char *path);
+ISLBM_API int islbm_write_tecplot_plt(islbm_handle *h, const char *path);
+ISLBM_API int islbm_write_monitor(islbm_handle *h, const char *path, int step);
 
 ISLBM_API int islbm_destroy(islbm_handle *h);
 

@@ -412,7 +412,7 @@ int islbm_default_params(islbm_params *p) {
     p->Re = 700.0; p->Uref = 0.05;
     p->NDTFRC = 10000;
     p->precision = ISLBM_FP64;
-    p->les_cs = 0.0; p->alpha = 1.0;
+    p->les_cs = 0.0; p->alpha = 1.0; p->geometry = 0;
     p->init_mode = 1; p->seed = 1234ULL; p->perturb = 0.01;
     p->mass_interval = 0; p->bfl_mode = 0; p->device = 0;
     p->kernel = ISLBM_KERNEL_AUTO;

@@ -49,6 +49,7 @@ void weights7(double *dst, size_t stride, size_t store, double pos, const double
 }  // namespace
 
 double Geometry::hill(double Y) const {
+    if (channel) return 0.0;   // ChannelFunction, C/model.h:70-73
     double Yb = Y;
     if (Y < 0.0) Yb = Y + LY; else if (Y > LY) Yb = Y - LY;
     if (alpha != 1.0) {
@@ -89,6 +90,7 @@ int validate(const islbm_params &p) {
     if (p.precision < ISLBM_FP64 || p.precision > ISLBM_BF16_DEV) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.les_cs < 0 || !(p.alpha > 0) || p.init_mode < 0 || p.init_mode > 1) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.mass_interval < 0 || p.bfl_mode < 0 || p.bfl_mode > 1) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (p.geometry < 0 || p.geometry > 1) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.kernel < ISLBM_KERNEL_AUTO || p.kernel > ISLBM_KERNEL_TILED) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.alpha != 1.0 && p.LY < 2.0*kBreak[5]*p.alpha) return ISLBM_ERR_INVALID_ARGUMENT;
     return ISLBM_OK;
@@ -99,7 +101,7 @@ int Geometry::build(const islbm_params &p) {
     if (st != ISLBM_OK) return st;
     NX = p.NX; NY = p.NY; NZ = p.NZ;
     NX6 = NX + 7; NYD6 = NY + 7; NZ6 = NZ + 6;
-    LX = p.LX; LY = p.LY; LZ = p.LZ; CFL = p.CFL; LXi = p.LXi; Re = p.Re; alpha = p.alpha;
+    LX = p.LX; LY = p.LY; LZ = p.LZ; CFL = p.CFL; LXi = p.LXi; Re = p.Re; alpha = p.alpha; channel = p.geometry == 1;
     minSize = ((LZ - 1.0)/(double)(NZ6 - 6))*CFL;
     dt = minSize;
     tau = 0.5 + 3.0*(p.Uref)/((double)Re*minSize);

@@ -26,6 +26,7 @@ struct Geometry {
     // grid (C/variables.h:10-19 with jp = 1)
     int NX = 0, NY = 0, NZ = 0, NX6 = 0, NYD6 = 0, NZ6 = 0;
     double LX = 0, LY = 0, LZ = 0, CFL = 0, LXi = 0, Re = 0, alpha = 1.0;
+    bool channel = false;   // flat channel: ChannelFunction (C/model.h:70-73) instead of the hill
     // derived constants (C/variables.h:22, 76, 97-101)
     double minSize = 0, dt = 0, tau = 0, niu = 0, Uref = 0, a_nonuni = 0;
     double force0 = 0;  // C/initialization.h:46

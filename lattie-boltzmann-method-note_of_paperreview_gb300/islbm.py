@@ -52,6 +52,7 @@ class Params(ctypes.Structure):
         ("device", ctypes.c_int),
         ("kernel", ctypes.c_int),
         ("hbm_budget_bytes", ctypes.c_size_t),
+        ("geometry", ctypes.c_int),
     ]
 
 
@@ -99,6 +100,9 @@ def load():
         "islbm_destroy": [vp],
         "islbm_diagnostics": [vp, dp],
         "islbm_diagnostics_noalloc": [vp, dp],
+        "islbm_write_tecplot_ascii": [vp, ctypes.c_char_p],
+        "islbm_write_tecplot_plt": [vp, ctypes.c_char_p],
+        "islbm_write_monitor": [vp, ctypes.c_char_p, ip],
         "islbm_checkpoint_write": [vp, ctypes.c_char_p, ip],
         "islbm_checkpoint_read": [vp, ctypes.c_char_p, ip],
         "islbm_stats_reset": [vp],
@@ -274,6 +278,15 @@ class Solver:
         out = (ctypes.c_double * 4)()
         check(self._L.islbm_diagnostics(self._h, out))
         return {"mass": out[0], "momentum_y": out[1], "kinetic_energy": out[2], "max_speed": out[3]}
+
+    def write_tecplot_ascii(self, path):
+        check(self._L.islbm_write_tecplot_ascii(self._h, os.fsencode(path)))
+
+    def write_tecplot_plt(self, path):
+        check(self._L.islbm_write_tecplot_plt(self._h, os.fsencode(path)))
+
+    def write_monitor(self, path, step):
+        check(self._L.islbm_write_monitor(self._h, os.fsencode(path), int(step)))
 
     def checkpoint_write(self, directory, rank=0):
         check(self._L.islbm_checkpoint_write(self._h, os.fsencode(directory), int(rank)))

@@ -106,6 +106,7 @@ static double hill_reference(double LY, double Y) {
 /* Steepness extension (not in the reference): the footprint is stretched by alpha, the
  * height is kept; alpha == 1 returns the reference hill exactly. */
 static double hill(const ora_t *o, double Y) {
+    if (o->p.geometry == 1) return 0.0;   /* ChannelFunction, C/model.h:70-73 */
     const double alpha = o->p.alpha;
     if (alpha == 1.0) return hill_reference(o->LY, Y);
     double Yb = Y;

@@ -28,6 +28,7 @@ typedef struct ora_params {
     double les_cs;           /* Smagorinsky constant, 0 = off */
     double alpha;            /* hill steepness (1 = reference hill) */
     int threads;             /* OpenMP threads, 0 = runtime default */
+    int geometry;            /* 0 hill (C/model.h:4-68), 1 flat channel (ChannelFunction, C/model.h:70-73) */
 } ora_params;
 
 typedef struct ora ora_t;

@@ -28,14 +28,15 @@ class OraParams(ctypes.Structure):
         ("les_cs", ctypes.c_double),
         ("alpha", ctypes.c_double),
         ("threads", ctypes.c_int),
+        ("geometry", ctypes.c_int),
     ]
 
 
 def make_params(nx, ny, nz, re=700.0, ub=0.05, ndtfrc=100, init_mode=1, seed=1234, amp=0.01,
-                mass_interval=0, bfl_mode=0, les_cs=0.0, alpha=1.0, threads=0):
+                mass_interval=0, bfl_mode=0, les_cs=0.0, alpha=1.0, threads=0, geometry=0):
     return OraParams(nx, ny, nz, 4.5, 9.0, 3.036, 0.6, 10.0, float(re), float(ub), int(ndtfrc),
                      int(init_mode), int(seed), float(amp), int(mass_interval), int(bfl_mode),
-                     float(les_cs), float(alpha), int(threads))
+                     float(les_cs), float(alpha), int(threads), int(geometry))
 
 
 _lib = None
