@@ -13,11 +13,11 @@ WEIGHT_TABLES = ["XPara0", "XPara2", "YPara0", "YPara2", "XiF3", "XiF4", "XiF5",
                  "XiBFL4910", "YBFL15", "XiBFL15", "YBFL16", "XiBFL16"]
 
 
-@pytest.mark.parametrize("grid", [(8, 16, 16), (32, 64, 48), (16, 48, 24)])
-def test_tables_bit_exact(islbm_lib, oracle_mod, grid):
+@pytest.mark.parametrize("grid,geometry", [((8, 16, 16), 0), ((32, 64, 48), 0), ((16, 48, 24), 0), ((8, 16, 16), 1)])
+def test_tables_bit_exact(islbm_lib, oracle_mod, grid, geometry):
     nx, ny, nz = grid
-    p = islbm_lib.default_params(NX=nx, NY=ny, NZ=nz, Re=700.0, Uref=0.05, NDTFRC=100)
-    O = oracle_mod.Oracle(nx, ny, nz)
+    p = islbm_lib.default_params(NX=nx, NY=ny, NZ=nz, Re=700.0, Uref=0.05, NDTFRC=100, geometry=geometry)
+    O = oracle_mod.Oracle(nx, ny, nz, geometry=geometry)
     for nm in FLOAT_TABLES:
         assert np.array_equal(islbm_lib.host_table(p, nm), O.get(nm)), nm
     for nm in WEIGHT_TABLES:
