@@ -33,6 +33,9 @@ for _p in (ROOT, PKG):
         sys.path.insert(0, _p)
 
 METRIC = "ISLBM MLUPS & %HBM peak, mixed vs plain FP32 at stated err; serve p50/p99"
+# DRAM bytes of one launch of the FP32 step on this workload, from an ncu capture of the same
+# kernel (dram__bytes_read.sum + dram__bytes_write.sum: 529.3 MB + 440.6 MB)
+NCU_TRAFFIC_BYTES = 969.9e6
 CASE = dict(NX=128, NY=256, NZ=192, Re=2800.0, Uref=0.05, NDTFRC=100, les_cs=0.1)
 WORKLOAD = "periodic hill 256x128x192 (streamwise x spanwise x wall-normal), Re_h 2800, LES Cs 0.1, Ub 0.05"
 
@@ -295,7 +298,8 @@ def main():
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / peak, "traffic": NCU_TRAFFIC_BYTES, "traffic_unit": "bytes per launch (ncu)",
+                         "traffic_vs_algorithmic": NCU_TRAFFIC_BYTES / bytes_per_launch, "peak_kind": peak_kind,
                          "bytes_model": "2 x 19 x 4 B per node per step (read + write each population once)"},
             "clocks": clk.summary()}
     if rank == 0 and not args.no_mixed:
