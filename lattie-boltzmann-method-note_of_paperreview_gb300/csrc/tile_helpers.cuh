@@ -110,8 +110,8 @@ __device__ __forceinline__ int wrapi(int v, int n) {
 // BFL rows (C/evolution.h:505-572) for one node, reading the old populations from global
 // memory; rare (flagged wall rows only), kept out of line.
 template <class S>
-__device__ __noinline__ void bfl_node(const S *__restrict__ fo, const Tables<float> &T, const StepConst &k, int x, int y, int z,
-                                      float *F) {
+__device__ __forceinline__ void bfl_node_body(const S *__restrict__ fo, const Tables<float> &T, const StepConst &k, int x,
+                                              int y, int z, float *F) {
     const int NX = k.NX, NY = k.NY;
     const size_t N = (size_t)NX*NY*k.NZ;
     const int nb = 2*k.NYD6;
@@ -167,6 +167,13 @@ __device__ __noinline__ void bfl_node(const S *__restrict__ fo, const Tables<flo
         if (q > 0.5f) F[16] = lin(q, 17, 16);
         if (q < 0.5f) F[16] = y_xi(17, B_YB16, B_XIB16);
     }
+}
+
+// out of line for callers that keep it off their hot path
+template <class S>
+__device__ __noinline__ void bfl_node(const S *__restrict__ fo, const Tables<float> &T, const StepConst &k, int x, int y, int z,
+                                      float *F) {
+    bfl_node_body<S>(fo, T, k, x, y, z, F);
 }
 
 }  // namespace

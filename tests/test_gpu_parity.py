@@ -194,3 +194,4 @@ def test_tiled_wide_grid_vs_oracle(islbm_lib, oracle_mod):
     assert rel_l2(g["rho"], r["rho"]) <= 1e-5
     assert rel_l2(velocity(g), velocity(r)) <= 1e-4
 
+
