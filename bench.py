@@ -219,6 +219,17 @@ def serve_run(islbm, nreq, device):
             "error_vs_fp64": errs}
 
 
+def slowest_rank_ms(ms, world, device):
+    """Replicas: every rank ran the same workload; the job's time is the slowest rank's."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def rel_l2(a, b):
     import numpy as np
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
@@ -281,12 +292,7 @@ def main():
     with ClockSampler(local) as clk:
         r32 = device_run(islbm, torch, "fp32", args.steps, args.warmup, local)
     barrier()
-    ms = r32["ms"]
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = slowest_rank_ms(r32["ms"], world, "cuda")
     value = n * args.steps * world / (ms * 1e-3) / 1e6
     bytes_per_launch = 2 * 19 * 4 * n
     achieved = bytes_per_launch / (ms * 1e-3 / args.steps) / 1e9
