@@ -236,6 +236,44 @@ cudaError_t launch_init_state(const islbm_handle *h, void *f) {
     }
 }
 
+// Device forms of to_storage / from_storage (same operations, same rounding) for the unique
+// layout, so that host buffers move as FP64 without host-side conversion loops.
+template <class S>
+__global__ void to_storage_kernel(const double *__restrict__ src, S *__restrict__ dst, size_t n, double wq) {
+    for (size_t i = blockIdx.x*(size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x*blockDim.x)
+        dst[i] = to_s<S>(src[i], wq);
+}
+template <class S> __device__ __forceinline__ double from_s(S v, float wq);
+template <> __device__ __forceinline__ double from_s<double>(double v, float) { return v; }
+template <> __device__ __forceinline__ double from_s<float>(float v, float) { return (double)v; }
+template <> __device__ __forceinline__ double from_s<__half>(__half v, float wq) { return (double)__fadd_rn(__half2float(v), wq); }
+template <> __device__ __forceinline__ double from_s<__nv_bfloat16>(__nv_bfloat16 v, float wq) {
+    return (double)__fadd_rn(__bfloat162float(v), wq);
+}
+template <class S>
+__global__ void from_storage_kernel(const S *__restrict__ src, double *__restrict__ dst, size_t n, float wq) {
+    for (size_t i = blockIdx.x*(size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x*blockDim.x)
+        dst[i] = from_s<S>(src[i], wq);
+}
+
+template <class F>
+cudaError_t by_storage(int precision, F &&f) {
+    switch (precision) {
+    case ISLBM_FP64: return f(Tag<double>{});
+    case ISLBM_FP32: return f(Tag<float>{});
+    case ISLBM_FP16_DEV: return f(Tag<__half>{});
+    default: return f(Tag<__nv_bfloat16>{});
+    }
+}
+
+// the FP64 transfer buffer of a handle (N doubles, allocated on first use)
+cudaError_t xfer_buffer(islbm_handle *h) {
+    if (h->xfer) return cudaSuccess;
+    return cudaMalloc(&h->xfer, h->N*sizeof(double));
+}
+
+unsigned conv_grid(size_t n) { return (unsigned)std::min<size_t>(4096, (n + 255)/256); }
+
 // host <-> storage conversion of one population array
 void to_storage(int precision, int q, const double *src, void *dst, size_t n) {
     const double wq = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
@@ -281,6 +319,15 @@ int check_handle(const islbm_handle *h) { return h ? ISLBM_OK : ISLBM_ERR_INVALI
 
 int copy_macro(islbm_handle *h, int which, double *out, int layout) {
     const size_t N = h->N;
+    if (layout == ISLBM_LAYOUT_UNIQUE && h->celem == 4) {
+        // widen on the device and copy straight into the caller's buffer
+        CK(xfer_buffer(h));
+        from_storage_kernel<float><<<conv_grid(N), 256, 0, h->stream>>>((const float *)h->macros[which], h->xfer, N, 0.f);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(out, h->xfer, N*8, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return ISLBM_OK;
+    }
     std::vector<double> tmp(N);
     if (h->celem == 8) {
         CK(cudaMemcpyAsync(tmp.data(), h->macros[which], N*8, cudaMemcpyDeviceToHost, h->stream));
@@ -304,6 +351,7 @@ void free_handle_impl(islbm_handle *h) {
     if (h->tabmem) cudaFree(h->tabmem);
     if (h->ctrl) cudaFree(h->ctrl);
     if (h->stats) cudaFree(h->stats);
+    if (h->xfer) cudaFree(h->xfer);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -479,6 +527,19 @@ int islbm_get_population(islbm_handle *h, int q, double *out, int layout) {
     if (check_handle(h) || q < 0 || q > 18 || !out || layout < 0 || layout > 1) return ISLBM_ERR_INVALID_ARGUMENT;
     CK(cudaSetDevice(h->device));
     const size_t N = h->N;
+    if (layout == ISLBM_LAYOUT_UNIQUE) {
+        CK(xfer_buffer(h));
+        const float wq = q == 0 ? 1.0f/3.0f : (q < 7 ? 1.0f/18.0f : 1.0f/36.0f);
+        const void *src = (const char *)h->fbuf[h->cur] + (size_t)q*N*h->elem;
+        CK(by_storage(h->p.precision, [&](auto tag) {
+            using S = typename decltype(tag)::type;
+            from_storage_kernel<S><<<conv_grid(N), 256, 0, h->stream>>>((const S *)src, h->xfer, N, wq);
+            return cudaGetLastError();
+        }));
+        CK(cudaMemcpyAsync(out, h->xfer, N*8, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return ISLBM_OK;
+    }
     std::vector<char> stage(N*h->elem);
     CK(cudaMemcpyAsync(stage.data(), (const char *)h->fbuf[h->cur] + (size_t)q*N*h->elem, N*h->elem, cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
@@ -494,6 +555,22 @@ int islbm_set_populations(islbm_handle *h, const double *f19, int layout) {
     CK(cudaSetDevice(h->device));
     const size_t N = h->N;
     const size_t nref = (size_t)(h->p.NX + 7)*(h->p.NY + 7)*(h->p.NZ + 6);
+    if (layout == ISLBM_LAYOUT_UNIQUE) {
+        // FP64 up, narrowed to the storage format on the device
+        CK(xfer_buffer(h));
+        for (int q = 0; q < 19; q++) {
+            const double wq = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
+            CK(cudaMemcpyAsync(h->xfer, f19 + (size_t)q*N, N*8, cudaMemcpyHostToDevice, h->stream));
+            void *dst = (char *)h->fbuf[h->cur] + (size_t)q*N*h->elem;
+            CK(by_storage(h->p.precision, [&](auto tag) {
+                using S = typename decltype(tag)::type;
+                to_storage_kernel<S><<<conv_grid(N), 256, 0, h->stream>>>(h->xfer, (S *)dst, N, wq);
+                return cudaGetLastError();
+            }));
+        }
+        CK(cudaStreamSynchronize(h->stream));
+        return ISLBM_OK;
+    }
     std::vector<double> tmp(N);
     std::vector<char> stage(19*N*h->elem);
     for (int q = 0; q < 19; q++) {

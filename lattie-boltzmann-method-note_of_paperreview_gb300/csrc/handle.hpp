@@ -31,6 +31,7 @@ struct islbm_handle {
     bool use_tiled = false;
     double *stats = nullptr;   // time-average accumulators, ISLBM_STAT_COUNT x N (allocated on first use)
     long long stats_samples = 0;
+    double *xfer = nullptr;    // FP64 transfer buffer of N values for host copies (first use)
     TiledConst tiled{};
 };
 
