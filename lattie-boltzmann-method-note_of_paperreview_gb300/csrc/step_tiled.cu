@@ -33,11 +33,14 @@ namespace islbm {
 namespace {
 
 constexpr int NTHREADS = 128;
-constexpr int NSTAGES = 2;
+// Copy stages per tile: two for FP32 storage (two CTAs of 88 KB fit an SM), three for the
+// 2-byte formats, whose stages are half the size: the next-but-one plane is then in flight
+// while a plane is filtered.
+template <class S> constexpr int stages_for() { return sizeof(S) == 2 ? 3 : 2; }
 
 // Shared-memory layout of one tile for a spanwise width NXC (a power of two): all offsets are
 // compile-time constants so every shared-memory address is a base plus an immediate.
-//   stage s (NSTAGES of them): population q in [1, 18] as `rows(q)` rows of NXC values
+//   stage s (NS of them): population q in [1, 18] as `rows(q)` rows of NXC values
 //   (TY rows, or TY + 6 with the streamwise halo), then the target's xi weights (TY x 64
 //   floats) and f0 row (TY x NXC values); then ybuf [4][TY][NXC] and xbuf [10][TY][NXC] floats,
 //   then the stage mbarriers.
@@ -47,6 +50,7 @@ struct Lay {
     static constexpr int TY = NTHREADS/NXC;
     static constexpr int LOG2NX = NXC == 8 ? 3 : NXC == 16 ? 4 : NXC == 32 ? 5 : NXC == 64 ? 6 : NXC == 128 ? 7 : 8;
     static constexpr int EB = (int)sizeof(S);
+    static constexpr int NS = stages_for<S>();
     static constexpr bool wide(int q) { return q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15; }
     static constexpr int rows(int q) { return q == 0 ? 0 : (wide(q) ? TY + 6 : TY); }
     static constexpr int up16(int v) { return (v + 15)/16*16; }
@@ -65,10 +69,10 @@ struct Lay {
     static constexpr int f0_off = up16(w_off + TY*64*4);
     static constexpr int stage_bytes = (up16(f0_off + TY*NX*EB) + 127)/128*128;
     static constexpr unsigned tgt_bytes = (unsigned)(TY*64*4 + TY*NX*EB);
-    static constexpr int ybuf_off = NSTAGES*stage_bytes;
+    static constexpr int ybuf_off = NS*stage_bytes;
     static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
     static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
-    static constexpr int flag_off = bar_off + NSTAGES*8;   // CTA-wide "a wait timed out" flag
+    static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag
     static constexpr int smem_bytes = flag_off + 16;
 };
 
@@ -255,7 +259,7 @@ struct TiledKernel {
     __device__ __forceinline__ void drain(unsigned char *smem, unsigned parity, int tid) const {
         if (tid != 0) return;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
-        for (int s = 0; s < NSTAGES; s++) {
+        for (int s = 0; s < LY::NS; s++) {
             if (!((parity >> (PEND + s)) & 1u)) continue;
             const unsigned ph = (parity >> (PPAR + s)) & 1u;
             for (int it = 0; it < (1 << 22); ++it) {
@@ -287,7 +291,7 @@ struct TiledKernel {
     __device__ __forceinline__ Slot plane(int i, int p, int p1, int y0, unsigned char *smem, unsigned &parity, bool &faulted,
                                           const Lane &L) const {
         constexpr int NX = LY::NX, TY = LY::TY;
-        const int s = i % NSTAGES;
+        const int s = i % LY::NS;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         float *ybuf = (float *)(smem + LY::ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
         float *xbuf = (float *)(smem + LY::xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
@@ -318,8 +322,8 @@ struct TiledKernel {
             ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
         }
         __syncthreads();
-        // every thread has finished plane i-1: its stage can take plane i + NSTAGES - 1
-        if (p + NSTAGES - 1 <= p1) issue(smem, (i + NSTAGES - 1) % NSTAGES, p + NSTAGES - 1, y0, L, parity);
+        // every thread has finished plane i-1: its stage can take plane i + NS - 1
+        if (p + LY::NS - 1 <= p1) issue(smem, (i + LY::NS - 1) % LY::NS, p + LY::NS - 1, y0, L, parity);
         {   // spanwise filter: two nodes of one row, five directions of one departure side
             const int m = NX - 1;
             const int x0 = L.xx0;
@@ -410,7 +414,7 @@ struct TiledKernel {
         const int y0 = tile*TY;
         const int p1 = NZ - 1;
         __syncthreads();   // every thread is done with every stage of the previous column
-        for (int s = 0; s < NSTAGES - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity);
+        for (int s = 0; s < LY::NS - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity);
         const int y = y0 + L.yl;
         // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
 #pragma unroll 1
@@ -425,7 +429,7 @@ struct TiledKernel {
         for (int p = 7; p <= NZ - 1; p++) {
             const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
             ring_store(R, ph, v);
-            const unsigned char *stage = smem + (size_t)(p % NSTAGES)*LY::stage_bytes;
+            const unsigned char *stage = smem + (size_t)(p % LY::NS)*LY::stage_bytes;
             const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
             float F[19];
             xi_combine_phase(ph, R, wv, F);
@@ -443,7 +447,7 @@ struct TiledKernel {
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         const Lane L = lane();
         if (L.tid == 0) {
-            for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
+            for (int s = 0; s < LY::NS; s++) mbar_init(&bars[s], 1);
             *(volatile int *)(smem + LY::flag_off) = 0;
             fence_mbar_init();
         }
@@ -496,7 +500,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
     uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
     const int tid = threadIdx.x;
     if (tid == 0) {
-        for (int s = 0; s < NSTAGES; s++) mbar_init(&bars[s], 1);
+        for (int s = 0; s < LY::NS; s++) mbar_init(&bars[s], 1);
         *(volatile int *)(smem + LY::flag_off) = 0;
         fence_mbar_init();
     }
@@ -616,7 +620,7 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     off = up16(off + (size_t)tc.TY*k.NX*eb);
     tc.tgt_bytes = (unsigned)(tc.TY*64*sizeof(float) + tc.TY*k.NX*eb);
     tc.stage_bytes = (off + 127)/128*128;
-    tc.ybuf_off = NSTAGES*tc.stage_bytes;
+    tc.ybuf_off = (precision == ISLBM_FP32 ? 2 : 3)*tc.stage_bytes;
     tc.xbuf_off = tc.ybuf_off + (size_t)4*tc.TY*k.NX*sizeof(float);
     tc.bar_off = tc.xbuf_off + (size_t)10*tc.TY*k.NX*sizeof(float);
     tc.smem_bytes = precision == ISLBM_FP32 ? smem_for<float>(k.NX) : smem_for<__half>(k.NX);
