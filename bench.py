@@ -178,19 +178,30 @@ def accuracy_run(islbm, device, steps=200):
     min_size = (3.036 - 1.0) / CASE["NZ"] * 0.6
     kw = dict(CASE)
     kw["Re"] = 3.0 * CASE["Uref"] / (0.5 * min_size)
-    out, ref = {}, None
+    # streamwise stations x/h = 0.5, 2, 4, 6, 8 of the profiles (rows of the uniform y mesh)
+    rows = [int(round(st * CASE["NY"] / 9.0)) % CASE["NY"] for st in (0.5, 2.0, 4.0, 6.0, 8.0)]
+    out, ref, ref_prof, ref_cf = {}, None, None, None
     for prec in ("fp64", "fp32", "fp16", "bf16"):
         with islbm.Solver(islbm.default_params(precision=prec, device=device, **kw)) as s:
             m0 = s.diagnostics()["mass"]
-            s.step(steps)
+            s.stats_reset()
+            for _ in range(steps // 10):   # time averages over the run, one sample every 10 steps
+                s.step(10)
+                s.stats_accumulate()
             f = s.fields()
             m1 = s.diagnostics()["mass"]
+            prof = np.stack([[s.stats_profile(q, y) for y in rows] for q in ("U", "V", "W")])
+            cf = s.stats_wall_shear()
         u = np.stack([f[c] for c in "uvw"])
         if ref is None:
-            ref = u
+            ref, ref_prof, ref_cf = u, prof, cf
         out[prec] = {"rel_l2_u_vs_fp64": rel_l2(u, ref), "max_abs_u_over_ub": float(np.abs(u - ref).max() / CASE["Uref"]),
+                     "time_avg_profiles_max_abs_err_over_ub": float(np.abs(prof - ref_prof).max() / CASE["Uref"]),
+                     "wall_cf_max_abs_err": float(np.abs(cf - ref_cf).max()), "wall_cf_max": float(np.abs(ref_cf).max()),
                      "mass_drift_rel": (m1 - m0) / m0}
-    return {"case": "256x128x192, LES Cs 0.1, tau 1.0 (Re_h %.2f)" % kw["Re"], "steps": steps, "errors": out}
+    return {"case": "256x128x192, LES Cs 0.1, tau 1.0 (Re_h %.2f)" % kw["Re"], "steps": steps,
+            "profiles": "spanwise-averaged time means of u, v, w at x/h = 0.5, 2, 4, 6, 8 (%d samples)" % (steps // 10),
+            "errors": out}
 
 
 def serve_run(islbm, nreq, device):

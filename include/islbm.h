@@ -184,6 +184,11 @@ ISLBM_API int islbm_stats_mean(islbm_handle *h, int quantity, double *out, int l
 /* spanwise average of the time mean at streamwise row y (0 <= y < NY): NZ values, wall-normal
  * index 0 at the hill surface (the profiles of C/fileIO.h:118-249) */
 ISLBM_API int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *out);
+/* skin friction along the lower wall from the time means: cf[y] = 2 niu (d u_t / d n) / Uref^2
+ * for every streamwise row y (NY values), u_t the spanwise-averaged mean velocity tangential to
+ * the hill surface, its wall-normal gradient from a quadratic through the wall (half a cell
+ * below the first node, where the half-way bounce-back puts it) and the two lowest nodes. */
+ISLBM_API int islbm_stats_wall_shear(islbm_handle *h, double *cf);
 
 /* Checkpoint / restart in the reference's files (OutputData / InitialUsingBkpData,
  * C/fileIO.h:52-67, 262-266, 298-354): <dir>/{rho,u,v,w,f0..f18}_<rank>.bin as raw FP64 arrays

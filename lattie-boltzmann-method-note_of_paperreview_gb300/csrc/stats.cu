@@ -129,4 +129,43 @@ int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *out) {
     return ISLBM_OK;
 }
 
+int islbm_stats_wall_shear(islbm_handle *h, double *cf) {
+    if (!h || !cf) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->stats || h->stats_samples == 0) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics samples");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    const int NX = h->p.NX, NY = h->p.NY;
+    const size_t plane = (size_t)NX*NY;
+    // the two lowest planes (z = 0, 1) of the time sums of V and W
+    std::vector<double> v(2*plane), w(2*plane);
+    e = cudaMemcpyAsync(v.data(), h->stats + (size_t)ISLBM_STAT_V*h->N, 2*plane*sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w.data(), h->stats + (size_t)ISLBM_STAT_W*h->N, 2*plane*sizeof(double),
+                            cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return report_cuda(e, "statistics wall read");
+    const Geometry &g = h->g;
+    const double inv = 1.0/((double)h->stats_samples*NX);
+    for (int y = 0; y < NY; y++) {
+        const int j = y + 3;
+        // wall height z_h[j*NZ6 + 2] and its streamwise slope (central difference, periodic rows)
+        const double zw = g.z[(size_t)j*g.NZ6 + 2];
+        const double zm = g.z[(size_t)(j - 1)*g.NZ6 + 2], zp = g.z[(size_t)(j + 1)*g.NZ6 + 2];
+        const double slope = (zp - zm)/(g.y[j + 1] - g.y[j - 1]);
+        const double norm = std::sqrt(1.0 + slope*slope);
+        double ut[2], d[2];
+        for (int k = 0; k < 2; k++) {
+            double sv = 0.0, sw = 0.0;
+            for (int x = 0; x < NX; x++) { sv += v[(size_t)k*plane + (size_t)y*NX + x]; sw += w[(size_t)k*plane + (size_t)y*NX + x]; }
+            ut[k] = (sv*inv + slope*sw*inv)/norm;                       // tangential mean velocity
+            d[k] = (g.z[(size_t)j*g.NZ6 + 3 + k] - zw)/norm;            // distance from the wall
+        }
+        // u(d) = a d + b d^2 through the wall (u = 0) and the two lowest nodes
+        const double a = (ut[0]*d[1]*d[1] - ut[1]*d[0]*d[0])/(d[0]*d[1]*(d[1] - d[0]));
+        cf[y] = 2.0*g.niu*a/(g.Uref*g.Uref);
+    }
+    return ISLBM_OK;
+}
+
 }  // extern "C"

@@ -33,10 +33,9 @@ namespace islbm {
 namespace {
 
 constexpr int NTHREADS = 128;
-// Copy stages per tile: two for FP32 storage (two CTAs of 88 KB fit an SM), three for the
-// 2-byte formats, whose stages are half the size: the next-but-one plane is then in flight
-// while a plane is filtered.
-template <class S> constexpr int stages_for() { return sizeof(S) == 2 ? 3 : 2; }
+// Copy stages per tile: the next plane is in flight while one is filtered (a third stage for
+// the 2-byte formats, which would fit, measured no faster on GB300).
+template <class S> constexpr int stages_for() { return 2; }
 
 // Shared-memory layout of one tile for a spanwise width NXC (a power of two): all offsets are
 // compile-time constants so every shared-memory address is a base plus an immediate.
@@ -620,7 +619,7 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     off = up16(off + (size_t)tc.TY*k.NX*eb);
     tc.tgt_bytes = (unsigned)(tc.TY*64*sizeof(float) + tc.TY*k.NX*eb);
     tc.stage_bytes = (off + 127)/128*128;
-    tc.ybuf_off = (precision == ISLBM_FP32 ? 2 : 3)*tc.stage_bytes;
+    tc.ybuf_off = 2*tc.stage_bytes;
     tc.xbuf_off = tc.ybuf_off + (size_t)4*tc.TY*k.NX*sizeof(float);
     tc.bar_off = tc.xbuf_off + (size_t)10*tc.TY*k.NX*sizeof(float);
     tc.smem_bytes = precision == ISLBM_FP32 ? smem_for<float>(k.NX) : smem_for<__half>(k.NX);

@@ -110,6 +110,7 @@ def load():
         "islbm_stats_samples": [vp, ctypes.POINTER(ctypes.c_longlong)],
         "islbm_stats_mean": [vp, ip, vp, ip],
         "islbm_stats_profile": [vp, ip, ip, vp],
+        "islbm_stats_wall_shear": [vp, vp],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
@@ -317,6 +318,12 @@ class Solver:
         q = STATS.index(quantity) if isinstance(quantity, str) else int(quantity)
         out = np.zeros(self.params.NZ, dtype=np.float64)
         check(self._L.islbm_stats_profile(self._h, q, int(y), out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def stats_wall_shear(self):
+        """Skin friction coefficient along the lower wall (NY values) from the time means."""
+        out = np.zeros(self.params.NY, dtype=np.float64)
+        check(self._L.islbm_stats_wall_shear(self._h, out.ctypes.data_as(ctypes.c_void_p)))
         return out
 
     def healthy(self):

@@ -40,3 +40,22 @@ def test_stats_match_host_sums(islbm_lib, precision):
         np.testing.assert_array_equal(ref_layout[3:-4, 3:-3, 3:-4].transpose(1, 0, 2), s.stats_mean("U"))
         s.stats_reset()
         assert s.stats_samples() == 0
+
+
+def test_wall_shear_of_poiseuille(islbm_lib):
+    """Flat channel at steady state: the force balance gives nu dv/dz = F LZ / 2 at the wall, so
+    cf = F LZ / Ub^2 on every row."""
+    islbm = islbm_lib
+    nx, ny, nz = 8, 16, 16
+    re = 3 * 0.05 / (0.5 * (3.036 - 1.0) / nz * 0.6)   # tau = 1
+    p = islbm.default_params(NX=nx, NY=ny, NZ=nz, Re=re, Uref=0.05, NDTFRC=10**9, precision="fp64", init_mode=0,
+                             geometry=1)
+    with islbm.Solver(p) as s:
+        s.step(12000)
+        s.stats_reset()
+        s.stats_accumulate()
+        cf = s.stats_wall_shear()
+        force = s.force
+    exact = force * 3.036 / 0.05 ** 2
+    assert cf.shape == (ny,)
+    assert np.abs(cf - exact).max() <= 0.03 * exact
