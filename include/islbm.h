@@ -171,10 +171,21 @@ typedef enum islbm_stat {
     ISLBM_STAT_PU, ISLBM_STAT_PV, ISLBM_STAT_PW, ISLBM_STAT_PP, ISLBM_STAT_KT,
     ISLBM_STAT_UUU, ISLBM_STAT_UUV, ISLBM_STAT_UUW, ISLBM_STAT_VVU, ISLBM_STAT_VVV, ISLBM_STAT_VVW,
     ISLBM_STAT_WWU, ISLBM_STAT_WWV, ISLBM_STAT_WWW,
-    ISLBM_STAT_COUNT
+    ISLBM_STAT_COUNT,
+    /* squared velocity gradients (MeanDerivatives, C/statistics.h:176-222), accumulated when
+     * enabled with islbm_stats_gradients */
+    ISLBM_STAT_DUDX2 = ISLBM_STAT_COUNT, ISLBM_STAT_DUDY2, ISLBM_STAT_DUDZ2,
+    ISLBM_STAT_DVDX2, ISLBM_STAT_DVDY2, ISLBM_STAT_DVDZ2,
+    ISLBM_STAT_DWDX2, ISLBM_STAT_DWDY2, ISLBM_STAT_DWDZ2,
+    ISLBM_STAT_ALL
 } islbm_stat;
 /* zero the sums (allocating them on first use) */
 ISLBM_API int islbm_stats_reset(islbm_handle *h);
+/* also accumulate the nine squared velocity gradients (on = 1), from the next reset on: x and y
+ * derivatives by the reference's fourth-order central differences, z derivatives by the
+ * five-point Lagrange derivative through the column's own wall-normal nodes (the reference
+ * indexes its five z weights, ZSlopePara, by k only and never fills them). */
+ISLBM_API int islbm_stats_gradients(islbm_handle *h, int on);
 /* add one sample (the fields of the last step); asynchronous on the handle's stream */
 ISLBM_API int islbm_stats_accumulate(islbm_handle *h);
 ISLBM_API int islbm_stats_samples(islbm_handle *h, long long *samples);

@@ -351,6 +351,7 @@ void free_handle_impl(islbm_handle *h) {
     if (h->tabmem) cudaFree(h->tabmem);
     if (h->ctrl) cudaFree(h->ctrl);
     if (h->stats) cudaFree(h->stats);
+    if (h->zslope) cudaFree(h->zslope);
     if (h->xfer) cudaFree(h->xfer);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;

@@ -31,6 +31,10 @@ struct islbm_handle {
     bool use_tiled = false;
     double *stats = nullptr;   // time-average accumulators, ISLBM_STAT_COUNT x N (allocated on first use)
     long long stats_samples = 0;
+    int stats_grad = 0;        // gradient quantities requested (ISLBM_STAT_ALL sums instead of COUNT)
+    int stats_nq = 0;          // quantities held by the current allocation of `stats`
+    double *zslope = nullptr;  // five wall-normal derivative weights per (z, y) node
+
     double *xfer = nullptr;    // FP64 transfer buffer of N values for host copies (first use)
     TiledConst tiled{};
 };

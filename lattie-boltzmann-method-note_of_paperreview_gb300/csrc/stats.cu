@@ -34,10 +34,86 @@ __global__ void stats_kernel(const C *__restrict__ rho, const C *__restrict__ u,
     }
 }
 
+// Squared velocity gradients of MeanVars' companion (MeanDerivatives, C/statistics.h:176-222):
+// x and y by the fourth-order central difference (8 (f[+1] - f[-1]) - (f[+2] - f[-2])) / 12 / h,
+// periodic; z by five weights per node over the nodes n .. n + 4 of its column,
+// n = clamp(z - 2, 0, NZ - 5).
+template <class C>
+__global__ void grad_kernel(const C *__restrict__ u, const C *__restrict__ v, const C *__restrict__ w,
+                            const double *__restrict__ zs, double *__restrict__ acc, int NX, int NY, int NZ, double dx,
+                            double dy) {
+    const size_t n = (size_t)NX*NY*NZ;
+    for (size_t i = blockIdx.x*(size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x*blockDim.x) {
+        const int x = (int)(i % NX);
+        const int y = (int)((i/NX) % NY);
+        const int z = (int)(i/((size_t)NX*NY));
+        const size_t row = i - x, plane = (size_t)NX*NY;
+        const size_t col = i - (size_t)y*NX;   // (x, 0, z)
+        auto ddx = [&](const C *f) {
+            const double a = f[row + ((x + 1) % NX)] - (double)f[row + ((x - 1 + NX) % NX)];
+            const double b = f[row + ((x + 2) % NX)] - (double)f[row + ((x - 2 + NX) % NX)];
+            return (8.0*a - b)/12.0/dx;
+        };
+        auto ddy = [&](const C *f) {
+            const double a = f[col + (size_t)((y + 1) % NY)*NX] - (double)f[col + (size_t)((y - 1 + NY) % NY)*NX];
+            const double b = f[col + (size_t)((y + 2) % NY)*NX] - (double)f[col + (size_t)((y - 2 + NY) % NY)*NX];
+            return (8.0*a - b)/12.0/dy;
+        };
+        const int nb = min(max(z - 2, 0), NZ - 5);
+        const double *c = zs + ((size_t)z*NY + y)*5;
+        auto ddz = [&](const C *f) {
+            const size_t b0 = (size_t)nb*plane + (size_t)y*NX + x;
+            double s = 0.0;
+            for (int m = 0; m < 5; m++) s += c[m]*(double)f[b0 + (size_t)m*plane];
+            return s;
+        };
+        const double g[9] = {ddx(u), ddy(u), ddz(u), ddx(v), ddy(v), ddz(v), ddx(w), ddy(w), ddz(w)};
+#pragma unroll
+        for (int q = 0; q < 9; q++) acc[(size_t)(ISLBM_STAT_DUDX2 + q)*n + i] += g[q]*g[q];
+    }
+}
+
+// derivative at t of the Lagrange polynomial through the five nodes zn, weight of node m
+double lagrange_slope(const double *zn, int m, double t) {
+    double s = 0.0;
+    for (int l = 0; l < 5; l++) {
+        if (l == m) continue;
+        double p = 1.0/(zn[m] - zn[l]);
+        for (int i = 0; i < 5; i++)
+            if (i != m && i != l) p *= (t - zn[i])/(zn[m] - zn[i]);
+        s += p;
+    }
+    return s;
+}
+
 }  // namespace
 }  // namespace islbm
 
 using namespace islbm;
+
+extern "C" int islbm_stats_gradients(islbm_handle *h, int on) {
+    if (!h || on < 0 || on > 1) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (h->p.NZ < 5) return report_status(ISLBM_ERR_NOT_SUPPORTED, "gradient statistics need NZ >= 5");
+    h->stats_grad = on;
+    if (on && !h->zslope) {
+        const Geometry &g = h->g;
+        const int NY = h->p.NY, NZ = h->p.NZ;
+        std::vector<double> w((size_t)NZ*NY*5);
+        for (int z = 0; z < NZ; z++)
+            for (int y = 0; y < NY; y++) {
+                const int j = y + 3, nb = std::min(std::max(z - 2, 0), NZ - 5);
+                double zn[5];
+                for (int m = 0; m < 5; m++) zn[m] = g.z[(size_t)j*g.NZ6 + 3 + nb + m];
+                const double t = g.z[(size_t)j*g.NZ6 + 3 + z];
+                for (int m = 0; m < 5; m++) w[((size_t)z*NY + y)*5 + m] = lagrange_slope(zn, m, t);
+            }
+        cudaError_t e = cudaSetDevice(h->device);
+        if (e == cudaSuccess) e = cudaMalloc(&h->zslope, w.size()*sizeof(double));
+        if (e == cudaSuccess) e = cudaMemcpy(h->zslope, w.data(), w.size()*sizeof(double), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return report_cuda(e, "gradient weights");
+    }
+    return ISLBM_OK;
+}
 
 extern "C" {
 
@@ -45,10 +121,13 @@ int islbm_stats_reset(islbm_handle *h) {
     if (!h) return ISLBM_ERR_INVALID_ARGUMENT;
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
-    const size_t bytes = (size_t)ISLBM_STAT_COUNT*h->N*sizeof(double);
+    const int nq = h->stats_grad ? ISLBM_STAT_ALL : ISLBM_STAT_COUNT;
+    const size_t bytes = (size_t)nq*h->N*sizeof(double);
+    if (h->stats && h->stats_nq != nq) { cudaFree(h->stats); h->stats = nullptr; }
     if (!h->stats) {
         e = cudaMalloc(&h->stats, bytes);
         if (e != cudaSuccess) { h->stats = nullptr; return report_cuda(e, "cudaMalloc(statistics)"); }
+        h->stats_nq = nq;
     }
     e = cudaMemsetAsync(h->stats, 0, bytes, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -78,6 +157,18 @@ int islbm_stats_accumulate(islbm_handle *h) {
                                                          (const float *)h->macros[2], (const float *)h->macros[3],
                                                          h->stats, h->N);
     e = cudaGetLastError();
+    if (e == cudaSuccess && h->stats_nq == ISLBM_STAT_ALL) {
+        const double dx = h->p.LX/h->p.NX, dy = h->p.LY/h->p.NY;
+        if (h->celem == 8)
+            grad_kernel<double><<<grid, 256, 0, h->stream>>>((const double *)h->macros[1], (const double *)h->macros[2],
+                                                             (const double *)h->macros[3], h->zslope, h->stats,
+                                                             h->p.NX, h->p.NY, h->p.NZ, dx, dy);
+        else
+            grad_kernel<float><<<grid, 256, 0, h->stream>>>((const float *)h->macros[1], (const float *)h->macros[2],
+                                                            (const float *)h->macros[3], h->zslope, h->stats,
+                                                            h->p.NX, h->p.NY, h->p.NZ, dx, dy);
+        e = cudaGetLastError();
+    }
     if (e != cudaSuccess) return report_cuda(e, "statistics kernel launch");
     h->stats_samples++;
     return ISLBM_OK;
@@ -90,7 +181,7 @@ int islbm_stats_samples(islbm_handle *h, long long *samples) {
 }
 
 int islbm_stats_mean(islbm_handle *h, int quantity, double *out, int layout) {
-    if (!h || !out || quantity < 0 || quantity >= ISLBM_STAT_COUNT || layout < 0 || layout > 1)
+    if (!h || !out || quantity < 0 || quantity >= (h->stats ? h->stats_nq : 0) || layout < 0 || layout > 1)
         return ISLBM_ERR_INVALID_ARGUMENT;
     if (!h->stats || h->stats_samples == 0) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics samples");
     cudaError_t e = cudaSetDevice(h->device);
@@ -108,7 +199,7 @@ int islbm_stats_mean(islbm_handle *h, int quantity, double *out, int layout) {
 }
 
 int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *out) {
-    if (!h || !out || quantity < 0 || quantity >= ISLBM_STAT_COUNT || y < 0 || y >= h->p.NY)
+    if (!h || !out || quantity < 0 || quantity >= (h->stats ? h->stats_nq : 0) || y < 0 || y >= h->p.NY)
         return ISLBM_ERR_INVALID_ARGUMENT;
     if (!h->stats || h->stats_samples == 0) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics samples");
     cudaError_t e = cudaSetDevice(h->device);

@@ -65,7 +65,8 @@ class SolveInfo(ctypes.Structure):
 
 # time-averaged quantities of islbm_stats_* (islbm_stat order)
 STATS = ["U", "V", "W", "P", "UU", "UV", "UW", "VV", "VW", "WW", "PU", "PV", "PW", "PP", "KT",
-         "UUU", "UUV", "UUW", "VVU", "VVV", "VVW", "WWU", "WWV", "WWW"]
+         "UUU", "UUV", "UUW", "VVU", "VVV", "VVW", "WWU", "WWV", "WWW",
+         "DUDX2", "DUDY2", "DUDZ2", "DVDX2", "DVDY2", "DVDZ2", "DWDX2", "DWDY2", "DWDZ2"]
 
 SOLVE_STATUS = {0: "queued", 1: "active", 2: "converged", 3: "capped", 4: "diverged", 5: "rejected"}
 
@@ -106,6 +107,7 @@ def load():
         "islbm_checkpoint_write": [vp, ctypes.c_char_p, ip],
         "islbm_checkpoint_read": [vp, ctypes.c_char_p, ip],
         "islbm_stats_reset": [vp],
+        "islbm_stats_gradients": [vp, ip],
         "islbm_stats_accumulate": [vp],
         "islbm_stats_samples": [vp, ctypes.POINTER(ctypes.c_longlong)],
         "islbm_stats_mean": [vp, ip, vp, ip],
@@ -297,6 +299,10 @@ class Solver:
 
     def stats_reset(self):
         check(self._L.islbm_stats_reset(self._h))
+
+    def stats_gradients(self, on=True):
+        """Also accumulate the squared velocity gradients (from the next reset on)."""
+        check(self._L.islbm_stats_gradients(self._h, int(bool(on))))
 
     def stats_accumulate(self):
         check(self._L.islbm_stats_accumulate(self._h))

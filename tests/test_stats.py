@@ -59,3 +59,55 @@ def test_wall_shear_of_poiseuille(islbm_lib):
     exact = force * 3.036 / 0.05 ** 2
     assert cf.shape == (ny,)
     assert np.abs(cf - exact).max() <= 0.03 * exact
+
+
+def lagrange_slope(zn, m, t):
+    s = 0.0
+    for l in range(5):
+        if l == m:
+            continue
+        p = 1.0 / (zn[m] - zn[l])
+        for i in range(5):
+            if i != m and i != l:
+                p *= (t - zn[i]) / (zn[m] - zn[i])
+        s += p
+    return s
+
+
+def host_gradients(islbm, p, f):
+    """MeanDerivatives' nine squared gradients (C/statistics.h:176-222) from the fields."""
+    nx, ny, nz = p.NX, p.NY, p.NZ
+    dx, dy = p.LX / nx, p.LY / ny
+    z = islbm.host_table(p, "z").reshape(ny + 7, nz + 6)[3:ny + 3, 3:nz + 3]   # (y, z)
+    out = {}
+    for c, a in (("U", f["u"]), ("V", f["v"]), ("W", f["w"])):
+        gx = (8 * (np.roll(a, -1, 2) - np.roll(a, 1, 2)) - (np.roll(a, -2, 2) - np.roll(a, 2, 2))) / 12 / dx
+        gy = (8 * (np.roll(a, -1, 1) - np.roll(a, 1, 1)) - (np.roll(a, -2, 1) - np.roll(a, 2, 1))) / 12 / dy
+        gz = np.zeros_like(a)
+        for k in range(nz):
+            nb = min(max(k - 2, 0), nz - 5)
+            for y in range(ny):
+                zn = z[y, nb:nb + 5]
+                w = [lagrange_slope(zn, m, z[y, k]) for m in range(5)]
+                gz[k, y, :] = sum(w[m] * a[nb + m, y, :] for m in range(5))
+        out["D%sDX2" % c], out["D%sDY2" % c], out["D%sDZ2" % c] = gx * gx, gy * gy, gz * gz
+    return out
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gradient_stats(islbm_lib, precision):
+    islbm = islbm_lib
+    p = islbm.default_params(NX=32, NY=64, NZ=48, Re=58.9, Uref=0.05, precision=precision, init_mode=1, seed=8)
+    with islbm.Solver(p) as s:
+        s.stats_gradients(True)
+        s.stats_reset()
+        acc = None
+        for _ in range(3):
+            s.step(5)
+            s.stats_accumulate()
+            g = host_gradients(islbm, p, s.fields())
+            acc = g if acc is None else {n: acc[n] + g[n] for n in g}
+        for name, ref in acc.items():
+            np.testing.assert_allclose(s.stats_mean(name), ref / 3, rtol=1e-9, atol=1e-12 * np.abs(ref).max(),
+                                       err_msg=name)
+        np.testing.assert_allclose(s.stats_mean("V"), s.stats_mean("V"))   # the base quantities stay
