@@ -50,8 +50,8 @@ typedef enum islbm_status {
 typedef enum islbm_precision {
     ISLBM_FP64 = 0,       /* distributions and arithmetic in FP64 (parity path) */
     ISLBM_FP32 = 1,       /* distributions and arithmetic in FP32 */
-    ISLBM_FP16_DEV = 2,   /* distributions stored as FP16 deviations f_i - w_i, FP32 arithmetic */
-    ISLBM_BF16_DEV = 3    /* distributions stored as BF16 deviations f_i - w_i, FP32 arithmetic */
+    ISLBM_FP16_DEV = 2,   /* distributions stored as FP16 deviations f_i - feq_i(rho 1, u = 0.05 e_y), FP32 arithmetic */
+    ISLBM_BF16_DEV = 3    /* distributions stored as BF16 deviations, as FP16_DEV, FP32 arithmetic */
 } islbm_precision;
 
 typedef enum islbm_layout {

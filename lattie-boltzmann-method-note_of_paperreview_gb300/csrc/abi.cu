@@ -207,12 +207,12 @@ __global__ void init_state_kernel(S *f, C *rho, C *u, C *v, C *w, size_t N, unsi
         }
         rho[i] = (C)rr; u[i] = (C)uu; v[i] = (C)vv; w[i] = (C)ww;
         const double udot = da(da(dm(uu, uu), dm(vv, vv)), dm(ww, ww));
-        f[i] = to_s<S>(dm(dm(W[0], rr), ds(1.0, dm(1.5, udot))), W[0]);
+        f[i] = to_s<S>(dm(dm(W[0], rr), ds(1.0, dm(1.5, udot))), dev_ref(0));
         for (int q = 1; q < 19; q++) {
             const double eu = da(da(dm((double)E[q][0], uu), dm((double)E[q][1], vv)), dm((double)E[q][2], ww));
             const double wq = W[q < 7 ? 1 : 2];
             const double fq = dm(dm(wq, rr), ds(da(da(1.0, dm(3.0, eu)), dm(dm(4.5, eu), eu)), dm(1.5, udot)));
-            f[(size_t)q*N + i] = to_s<S>(fq, wq);
+            f[(size_t)q*N + i] = to_s<S>(fq, dev_ref(q));
         }
     }
 }
@@ -276,7 +276,7 @@ unsigned conv_grid(size_t n) { return (unsigned)std::min<size_t>(4096, (n + 255)
 
 // host <-> storage conversion of one population array
 void to_storage(int precision, int q, const double *src, void *dst, size_t n) {
-    const double wq = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
+    const double wq = dev_ref(q);
     switch (precision) {
     case ISLBM_FP64: std::memcpy(dst, src, n*8); break;
     case ISLBM_FP32: for (size_t i = 0; i < n; i++) ((float *)dst)[i] = (float)src[i]; break;
@@ -285,7 +285,7 @@ void to_storage(int precision, int q, const double *src, void *dst, size_t n) {
     }
 }
 void from_storage(int precision, int q, const void *src, double *dst, size_t n) {
-    const float wq = q == 0 ? 1.0f/3.0f : (q < 7 ? 1.0f/18.0f : 1.0f/36.0f);
+    const float wq = (float)dev_ref(q);
     switch (precision) {
     case ISLBM_FP64: std::memcpy(dst, src, n*8); break;
     case ISLBM_FP32: for (size_t i = 0; i < n; i++) dst[i] = ((const float *)src)[i]; break;
@@ -530,7 +530,7 @@ int islbm_get_population(islbm_handle *h, int q, double *out, int layout) {
     const size_t N = h->N;
     if (layout == ISLBM_LAYOUT_UNIQUE) {
         CK(xfer_buffer(h));
-        const float wq = q == 0 ? 1.0f/3.0f : (q < 7 ? 1.0f/18.0f : 1.0f/36.0f);
+        const float wq = (float)dev_ref(q);
         const void *src = (const char *)h->fbuf[h->cur] + (size_t)q*N*h->elem;
         CK(by_storage(h->p.precision, [&](auto tag) {
             using S = typename decltype(tag)::type;
@@ -560,7 +560,7 @@ int islbm_set_populations(islbm_handle *h, const double *f19, int layout) {
         // FP64 up, narrowed to the storage format on the device
         CK(xfer_buffer(h));
         for (int q = 0; q < 19; q++) {
-            const double wq = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
+            const double wq = dev_ref(q);
             CK(cudaMemcpyAsync(h->xfer, f19 + (size_t)q*N, N*8, cudaMemcpyHostToDevice, h->stream));
             void *dst = (char *)h->fbuf[h->cur] + (size_t)q*N*h->elem;
             CK(by_storage(h->p.precision, [&](auto tag) {

@@ -4,7 +4,7 @@
 // Layout in HBM (one solve):
 //   populations  19 arrays of N = NX*NY*NZ unique nodes, f[q][z][y][x] (x fastest),
 //                two buffers (old/new) swapped every step; storage type S is double, float,
-//                or half/bfloat16 holding the deviation f - w_q;
+//                or half/bfloat16 holding the deviation f - ref_q (dev_ref below);
 //   weights      per-x and per-y Lagrange weights [a][x], [a][y] and the xi weights of the
 //                eight xi tables per (y, z), interleaved per stencil point a:
 //                [(z*NY + y)*64 + a*8 + t] (t = F3,4,5,6,15,16,17,18);
@@ -33,6 +33,19 @@ template <class C> __host__ __device__ __forceinline__ C lattice_w(int q) {
     return q == 0 ? C(1.0/3.0) : (q < 7 ? C(1.0/18.0) : C(1.0/36.0));
 }
 
+// Reference state of the deviation formats (FP16 / BF16 storage hold f_q - ref_q): the
+// equilibrium at rho = 1 and the bulk flow u = (0, 0.05, 0) of the benchmark cases, so that
+// the stored deviations are the small departures from the mean flow (about a third of the
+// departures from rest). Any constant per direction gives the same step up to rounding, since
+// every interpolation's weights sum to one and the reference is added back at each target.
+__host__ __device__ __forceinline__ double dev_ref(int q) {
+    const double u0 = 0.05;
+    const int ey = (q == 3 || q == 7 || q == 8 || q == 15 || q == 17) ? 1
+                 : (q == 4 || q == 9 || q == 10 || q == 16 || q == 18) ? -1 : 0;
+    const double w = q == 0 ? 1.0/3.0 : (q < 7 ? 1.0/18.0 : 1.0/36.0);
+    return w*(1.0 + 3.0*ey*u0 + 4.5*ey*ey*u0*u0 - 1.5*u0*u0);
+}
+
 __device__ __forceinline__ double to_c(double v) { return v; }
 __device__ __forceinline__ float to_c(float v) { return v; }
 __device__ __forceinline__ float to_c(__half v) { return __half2float(v); }
@@ -44,15 +57,15 @@ template <> __device__ __forceinline__ float from_c<float>(float v) { return v; 
 template <> __device__ __forceinline__ __half from_c<__half>(float v) { return __float2half_rn(v); }
 template <> __device__ __forceinline__ __nv_bfloat16 from_c<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
 
-// full population value from storage (deviation formats add the lattice weight back)
+// full population value from storage (deviation formats add the reference state back)
 template <class S> __device__ __forceinline__ typename Storage<S>::C load_f(const S *p, size_t i, int q) {
     using C = typename Storage<S>::C;
     const C v = to_c(__ldg(p + i));
-    if constexpr (Storage<S>::dev) return v + lattice_w<C>(q); else return v;
+    if constexpr (Storage<S>::dev) return v + (C)dev_ref(q); else return v;
 }
 template <class S> __device__ __forceinline__ void store_f(S *p, size_t i, int q, typename Storage<S>::C v) {
     using C = typename Storage<S>::C;
-    if constexpr (Storage<S>::dev) p[i] = from_c<S>(v - lattice_w<C>(q)); else p[i] = from_c<S>(v);
+    if constexpr (Storage<S>::dev) p[i] = from_c<S>(v - (C)dev_ref(q)); else p[i] = from_c<S>(v);
 }
 
 // Controller state, FP64 (Force_d, rho_modify_d, Ub_avg_d of the reference, reduced to

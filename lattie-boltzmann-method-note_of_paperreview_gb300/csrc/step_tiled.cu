@@ -170,7 +170,7 @@ struct TiledKernel {
         const size_t node = ((size_t)z*NY + y)*NX + x;
         if constexpr (Storage<S>::dev) {
 #pragma unroll
-            for (int q = 1; q < 19; q++) F[q] += lattice_w<float>(q);
+            for (int q = 1; q < 19; q++) F[q] += (float)dev_ref(q);
         }
         if (z == 0) {
             const S *b = fo + node;
@@ -432,7 +432,7 @@ struct TiledKernel {
             const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
             float F[19];
             xi_combine_phase(ph, R, wv, F);
-            F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, 1.f/3);
+            F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, (float)dev_ref(0));
             finish(F, L.xl, y, p - 3, sc, ub, mass);
             ph = ph == 6 ? 0 : ph + 1;
         }

@@ -74,7 +74,7 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned by
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
-// four consecutive stored values -> float (deviation formats add the lattice weight)
+// four consecutive stored values -> float (deviation formats add the reference state `w`)
 template <class S> __device__ __forceinline__ float4 ld4(const S *p, float w);
 template <> __device__ __forceinline__ float4 ld4<float>(const float *p, float) { return *(const float4 *)p; }
 template <> __device__ __forceinline__ float4 ld4<__half>(const __half *p, float w) {
@@ -90,7 +90,7 @@ template <> __device__ __forceinline__ float4 ld4<__nv_bfloat16>(const __nv_bflo
 template <class S> __device__ __forceinline__ float ld1(const S *p, float w) {
     if constexpr (Storage<S>::dev) return to_c(*p) + w; else return (float)*p;
 }
-// stored value as it is (the deviation f - w for the deviation formats): the interpolation
+// stored value as it is (the deviation f - ref for the deviation formats): the interpolation
 // weights of every filter sum to one, so filtering deviations and adding w once at the target
 // equals filtering full values up to rounding
 template <class S> __device__ __forceinline__ float ldv(const S *p) { return (float)to_c(*p); }

@@ -28,7 +28,7 @@ def test_stats_match_host_sums(islbm_lib, precision):
             q = host_quantities(s.fields())
             acc = q if acc is None else {n: acc[n] + q[n] for n in q}
         assert s.stats_samples() == 5
-        for i, name in enumerate(islbm.STATS):
+        for name in islbm.STATS[:24]:   # the MeanVars quantities (gradients not enabled)
             got = s.stats_mean(name)
             ref = acc[name] / 5
             scale = np.abs(ref).max()
