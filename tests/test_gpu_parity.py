@@ -216,3 +216,17 @@ def test_spanwise_translation_invariance_full_size(islbm_lib, prec):
         b.step(20)
         fb = b.populations()
     np.testing.assert_array_equal(fb, fa)
+
+
+def test_tiled_benchmark_grid_vs_oracle(islbm_lib, oracle_mod):
+    """The FP32 tiled step on the full 256x128x192 benchmark grid with Smagorinsky LES against
+    the oracle (the reference's step restated), 20 steps at tau = 1 where the scheme is stable."""
+    islbm = islbm_lib
+    min_size = (3.036 - 1.0) / 192 * 0.6
+    re = 3 * 0.05 / (0.5 * min_size)
+    steps = 20
+    g = solve(islbm, steps, NX=128, NY=256, NZ=192, Re=re, Uref=0.05, NDTFRC=10, les_cs=0.1, precision="fp32")
+    r = oracle_run(oracle_mod, steps, 128, 256, 192, re=re, ub=0.05, ndtfrc=10, les_cs=0.1)
+    assert rel_l2(g["rho"], r["rho"]) <= 2e-5
+    assert rel_l2(velocity(g), velocity(r)) <= 1e-4
+    assert abs(g["force"] - r["force"]) <= 1e-5 * abs(r["force"])
