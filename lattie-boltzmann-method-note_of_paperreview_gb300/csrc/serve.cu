@@ -296,14 +296,15 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
 }
 
 // Autotuner: candidate persistent-CTA counts for a batch, timed on one real step each.
+// Returns a status; the timed launches advance every member and are accounted for here.
 int tune(islbm_server *s, Group *g) {
     const std::string sig = std::to_string(g->precision) + "/" + std::to_string(g->NX) + "/" + std::to_string(g->les) +
                             "/" + std::to_string(g->nitems);
     auto it = s->tuned_grid.find(sig);
-    if (it != s->tuned_grid.end()) { g->grid = it->second; return 0; }
+    if (it != s->tuned_grid.end()) { g->grid = it->second; return ISLBM_OK; }
     // every member must have room for the tuning steps under its cap
     for (Solve *v : g->members)
-        if (v->max_steps - v->steps < 3) { g->grid = std::min(g->nitems, 2*s->sms); return 0; }
+        if (v->max_steps - v->steps < 3) { g->grid = std::min(g->nitems, 2*s->sms); return ISLBM_OK; }
     const int cand[3] = {std::min(g->nitems, s->sms), std::min(g->nitems, 2*s->sms), std::min(g->nitems, 4*s->sms)};
     float best = 1e30f;
     int best_grid = cand[0], launched = 0;
@@ -326,7 +327,7 @@ int tune(islbm_server *s, Group *g) {
     advanced(s, g, launched);   // the timed launches are real steps of every member
     s->tuned_grid[sig] = best_grid;
     g->grid = best_grid;
-    return launched;
+    return ISLBM_OK;
 }
 
 int run_group_chunk(islbm_server *s, Group *g, int steps) {
@@ -417,7 +418,7 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
         for (Group *g : groups) {
             if (!g->grid) {
                 st = tune(s, g);
-                if (st < 0) return ISLBM_ERR_CUDA;
+                if (st != ISLBM_OK) return st;
             }
             // the tuning steps count toward the chunk; what remains runs as one graph
             int left = steps;
