@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/islbm.h"
+#include "../../include/islbm_testing.h"
 #include "geometry.hpp"
 #include "step_launch.hpp"
 #include "step_tiled.hpp"
@@ -396,6 +397,7 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     k.tau = h->g.tau; k.les_C = p.les_cs*p.les_cs; k.dt = h->g.dt;
     k.Uref = h->g.Uref; k.beta = std::fmax(0.001, 3.0/(double)p.Re); k.area = (double)(p.LX*(p.LZ - 1.0));
     k.nnodes = (double)p.NX*(double)p.NY*(double)p.NZ;
+    k.drill_plane = -1;
 
     Ctrl c;
     std::memset(&c, 0, sizeof(c));
@@ -634,6 +636,13 @@ int islbm_sync(islbm_handle *h) {
     unsigned fault = 0;
     CK(cudaMemcpy(&fault, &h->ctrl->fault, sizeof(fault), cudaMemcpyDeviceToHost));
     if (fault) { g_last = "a shared-memory pipeline wait timed out in the step kernel"; return ISLBM_ERR_CUDA; }
+    return ISLBM_OK;
+}
+
+int islbm_fault_drill(islbm_handle *h, int plane) {
+    if (check_handle(h) || plane < -1 || plane >= h->p.NZ) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->use_tiled) { g_last = "the failure drill needs the tiled kernel"; return ISLBM_ERR_NOT_SUPPORTED; }
+    h->k.drill_plane = plane;
     return ISLBM_OK;
 }
 

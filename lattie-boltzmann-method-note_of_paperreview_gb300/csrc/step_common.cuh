@@ -103,6 +103,7 @@ struct StepConst {
     double dt;                 // = minSize
     double Uref, beta, area;   // controller: beta = max(0.001, 3/Re), area = LX*(LZ-1)
     double nnodes;
+    int drill_plane;           // test hook: the tiled kernel never copies this plane (-1: off)
 };
 
 enum { XI3 = 0, XI4, XI5, XI6, XI15, XI16, XI17, XI18 };

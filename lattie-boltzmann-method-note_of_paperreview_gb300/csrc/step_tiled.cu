@@ -280,6 +280,7 @@ struct TiledKernel {
     __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity) const {
         if ((L.tid & 31) >= 6) return;
         if (*(volatile int *)(smem + LY::flag_off)) return;
+        if (p == k.drill_plane) return;   // failure drill: this plane's copies never start
         fence_proxy_async();
         issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, y0, L.tid);
         if (L.tid == 0)

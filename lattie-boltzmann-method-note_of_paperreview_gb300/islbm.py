@@ -100,6 +100,7 @@ def load():
         "islbm_check_finite": [vp, ctypes.POINTER(ctypes.c_longlong)],
         "islbm_destroy": [vp],
         "islbm_diagnostics": [vp, dp],
+        "islbm_fault_drill": [vp, ip],
         "islbm_diagnostics_noalloc": [vp, dp],
         "islbm_write_tecplot_ascii": [vp, ctypes.c_char_p],
         "islbm_write_tecplot_plt": [vp, ctypes.c_char_p],
