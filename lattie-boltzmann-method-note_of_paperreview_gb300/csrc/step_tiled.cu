@@ -20,6 +20,7 @@
 //     similar heights and share the streamwise halo rows through L2.
 // Every value of the old populations is read from HBM about once per step (halo rows come
 // from L2); every new value is written once.
+#include <algorithm>
 #include <cstring>
 #include <type_traits>
 
@@ -71,80 +72,62 @@ struct Lay {
     static constexpr int ybuf_off = NS*stage_bytes;
     static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
     static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
-    static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag
-    static constexpr int smem_bytes = flag_off + 16;
+    static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag, then the TMEM address
+    // at least 46 KB, so that no more than four CTAs (4 x RING_COLS TMEM columns) share an SM
+    static constexpr int smem_bytes = flag_off + 16 > 46*1024 ? flag_off + 16 : 46*1024;
 };
 
-// Filtered values of one plane for the node of this thread (pairs of directions).
-struct Slot {
-    float2 r12, r34, r56, r78, r910, r1112, r1314, r1516, r1718;
-};
+// xi ring in tensor memory: each thread keeps the filtered values of the 7 planes of its
+// current window in its own TMEM lane; plane p sits in slot p mod 7:
+//   columns 16*s .. 16*s+15: pairs (3,4) (5,6) (15,16) (17,18) (7,9) (8,10) (11,13) (12,14),
+//   columns 112 + 2*s, +1: the spanwise-filtered F1, F2 of the plane (used by target p).
+// The pairs are chosen so that each pair's xi weights are adjacent in the weight row.
+constexpr int RING_COLS = 128;   // TMEM columns per CTA (power of two >= 32)
+__device__ __forceinline__ int ring_col(int p) { return 16*(p % 7); }
+__device__ __forceinline__ int r12_col(int p) { return 112 + 2*(p % 7); }
 
-// xi ring: the 7 planes of the current window in registers, slot (p mod 7) holding plane p.
-// Slot indices are compile-time constants in every access (the 7 window phases are
-// instantiated separately), so the ring is never shifted.
-struct Ring {
-    Slot s[7];
-};
-
-// xi combination of the window whose newest plane sits in slot NEW (oldest in NEW + 1).
-// The 64 weights of (y, z) are interleaved per stencil point c: (xi3, xi4, xi5, xi6, xi15,
-// xi16, xi17, xi18)[c], so one float4 yields the weight pairs of the packed FMAs.
-// Returns F[3..18] and F1, F2 of the plane three below the newest one.
-template <int NEW>
-__device__ __forceinline__ void xi_combine(const Ring &R, const float *wv_, float *F) {
+// xi combination of the window of planes b .. b+6 held in the TMEM ring (`tl` = this warp's
+// lane-quarter address). The 64 weights of (y, z) are interleaved per stencil point c:
+// (xi3, xi4, xi5, xi6, xi15, xi16, xi17, xi18)[c]. Writes F[3..18].
+__device__ __forceinline__ void xi_combine(uint32_t tl, int b, const float *wv_, float *F) {
     const float4 *wv = (const float4 *)wv_;
-    constexpr int O = (NEW + 1) % 7;   // slot of the oldest plane (c = 0)
-    P2 a34 = p2(0.f, 0.f), a56 = a34, a1516 = a34, a1718 = a34, a78 = a34, a910 = a34, a1112 = a34, a1314 = a34;
-#pragma unroll
-    for (int c = 0; c < 7; c++) {
-        const Slot &q = R.s[(O + c) % 7];
+    P2 a34 = p2(0.f, 0.f), a56 = a34, a1516 = a34, a1718 = a34, a79 = a34, a810 = a34, a1113 = a34, a1214 = a34;
+    auto acc = [&](const uint32_t (&q)[16], int c) {
         const float4 w = wv[2*c], u = wv[2*c + 1];
-        fma2(a34, p2(w.x, w.y), p2(q.r34));
-        fma2(a56, p2(w.z, w.w), p2(q.r56));
-        fma2(a1516, p2(u.x, u.y), p2(q.r1516));
-        fma2(a1718, p2(u.z, u.w), p2(q.r1718));
-        fma2(a78, p2(w.x, w.x), p2(q.r78));
-        fma2(a910, p2(w.y, w.y), p2(q.r910));
-        fma2(a1112, p2(w.z, w.z), p2(q.r1112));
-        fma2(a1314, p2(w.w, w.w), p2(q.r1314));
+        auto pr = [&](int i) { return p2(__uint_as_float(q[i]), __uint_as_float(q[i + 1])); };
+        fma2(a34, p2(w.x, w.y), pr(0));
+        fma2(a56, p2(w.z, w.w), pr(2));
+        fma2(a1516, p2(u.x, u.y), pr(4));
+        fma2(a1718, p2(u.z, u.w), pr(6));
+        fma2(a79, p2(w.x, w.y), pr(8));
+        fma2(a810, p2(w.x, w.y), pr(10));
+        fma2(a1113, p2(w.z, w.w), pr(12));
+        fma2(a1214, p2(w.z, w.w), pr(14));
+    };
+#pragma unroll
+    for (int c = 0; c < 6; c += 2) {
+        uint32_t q0[16], q1[16];
+        tmem_ld16(tl + ring_col(b + c), q0);
+        tmem_ld16(tl + ring_col(b + c + 1), q1);
+        tmem_wait_ld(q0, q1);
+        acc(q0, c);
+        acc(q1, c + 1);
     }
-    constexpr int MID = (NEW + 4) % 7;   // plane p - 3
-    F[1] = R.s[MID].r12.x; F[2] = R.s[MID].r12.y;
+    {
+        uint32_t q0[16];
+        tmem_ld16(tl + ring_col(b + 6), q0);
+        tmem_wait_ld(q0);
+        acc(q0, 6);
+    }
     float2 t;
     t = unp(a34); F[3] = t.x; F[4] = t.y;
     t = unp(a56); F[5] = t.x; F[6] = t.y;
-    t = unp(a78); F[7] = t.x; F[8] = t.y;
-    t = unp(a910); F[9] = t.x; F[10] = t.y;
-    t = unp(a1112); F[11] = t.x; F[12] = t.y;
-    t = unp(a1314); F[13] = t.x; F[14] = t.y;
     t = unp(a1516); F[15] = t.x; F[16] = t.y;
     t = unp(a1718); F[17] = t.x; F[18] = t.y;
-}
-
-// the window phase selects the instantiation
-__device__ __forceinline__ void xi_combine_phase(int ph, const Ring &R, const float *wv, float *F) {
-    switch (ph) {
-    case 0: xi_combine<0>(R, wv, F); break;
-    case 1: xi_combine<1>(R, wv, F); break;
-    case 2: xi_combine<2>(R, wv, F); break;
-    case 3: xi_combine<3>(R, wv, F); break;
-    case 4: xi_combine<4>(R, wv, F); break;
-    case 5: xi_combine<5>(R, wv, F); break;
-    default: xi_combine<6>(R, wv, F); break;
-    }
-}
-
-__device__ __forceinline__ void ring_store(Ring &R, int ph, const Slot &v) {
-    switch (ph) {
-    case 0: R.s[0] = v; break;
-    case 1: R.s[1] = v; break;
-    case 2: R.s[2] = v; break;
-    case 3: R.s[3] = v; break;
-    case 4: R.s[4] = v; break;
-    case 5: R.s[5] = v; break;
-    default: R.s[6] = v; break;
-    }
+    t = unp(a79); F[7] = t.x; F[9] = t.y;
+    t = unp(a810); F[8] = t.x; F[10] = t.y;
+    t = unp(a1113); F[11] = t.x; F[13] = t.y;
+    t = unp(a1214); F[12] = t.x; F[14] = t.y;
 }
 
 template <class S, bool LES, int NXC>
@@ -200,33 +183,15 @@ struct TiledKernel {
         if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
     }
 
-    // F1, F2 of a wall-cap target by direct spanwise gathers (the ring keeps only the plane
-    // three below the newest one)
-    __device__ __forceinline__ void cap_f12(int x, int y, int z, float *F) const {
-        constexpr int NX = LY::NX;
-        const int NY = k.NY;
-        const size_t N = (size_t)NX*NY*k.NZ;
-        const S *r1 = fo + 1*N + ((size_t)z*NY + y)*NX, *r2 = fo + 2*N + ((size_t)z*NY + y)*NX;
-        float a = 0, b = 0;
-#pragma unroll
-        for (int t = 0; t < 7; t++) {
-            const int xx = (x - 3 + t) & (NX - 1);
-            a += tc.wx0[t]*ldv<S>(r1 + xx);
-            b += tc.wx2[t]*ldv<S>(r2 + xx);
-        }
-        F[1] = a; F[2] = b;
-    }
-
     // Copy job q of a plane (1..18: population q, two pieces when the halo wraps; 19, 20: the
     // target's xi weights and f0 row). Jobs are spread over the four warps (job q on warp q & 3,
     // lane q >> 2) so that no warp serialises all the copy issues; thread 0 posts the expected
     // bytes (a copy may complete before that: the phase cannot end while the arrival is due).
-    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, int tid) const {
+    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int NY = k.NY, NZ = k.NZ;
         const size_t N = (size_t)NX*NY*NZ;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
-        const bool tgt = p >= 7 && p <= NZ - 1;
         if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         S *pops = (S *)stage;
         const int q = 4*(tid & 31) + (tid >> 5);   // lanes 0..5 only
@@ -274,22 +239,40 @@ struct TiledKernel {
         int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
 
+    // A piece of a column: targets ta .. tb-1 of tile rows y0 .. y0+TY-1, computed from source
+    // planes p0 .. p1 (target t uses planes b(t) .. b(t)+6, see window_base).
+    struct Piece {
+        int y0, ta, tb, p0, p1;
+    };
+    // first plane of target t's xi window (the reference's stencil base, clamped at the walls)
+    __device__ __forceinline__ int window_base(int t) const {
+        return t <= 3 ? 0 : (t >= k.NZ - 4 ? k.NZ - 7 : t - 3);
+    }
+    // targets 4 .. NZ-4 take their xi weights and f0 row from the stage of plane t + 3
+    __device__ __forceinline__ bool staged_target(int p, const Piece &P) const {
+        const int t = p - 3;
+        return t >= 4 && t <= k.NZ - 4 && t >= P.ta && t < P.tb;
+    }
+
     // After a CTA barrier, lanes 0..5 of every warp start the copies of plane p into stage s;
     // thread 0 (which posts the expected bytes) records the stage as pending. After a timed-out
     // wait anywhere in the CTA (the shared flag, written before the barrier) no copy starts.
-    __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, int y0, const Lane &L, unsigned &parity) const {
+    __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, const Piece &P, const Lane &L,
+                                          unsigned &parity) const {
         if ((L.tid & 31) >= 6) return;
         if (*(volatile int *)(smem + LY::flag_off)) return;
         if (p == k.drill_plane) return;   // failure drill: this plane's copies never start
         fence_proxy_async();
-        issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, y0, L.tid);
+        issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, P.y0, staged_target(p, P),
+                    L.tid);
         if (L.tid == 0)
             parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
     }
 
-    // One source plane: wait for its copies, filter, return the plane's slot values.
-    __device__ __forceinline__ Slot plane(int i, int p, int p1, int y0, unsigned char *smem, unsigned &parity, bool &faulted,
-                                          const Lane &L) const {
+    // One source plane (the i-th of its piece): wait for its copies, filter, and store the
+    // plane's values in the TMEM ring slot of plane p.
+    __device__ __forceinline__ void plane(int i, int p, const Piece &P, unsigned char *smem, unsigned &parity,
+                                          bool &faulted, const Lane &L, uint32_t tl) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int s = i % LY::NS;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
@@ -300,7 +283,6 @@ struct TiledKernel {
         if (mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted)) parity &= ~(1u << (PEND + s));
         else if (faulted) *(volatile int *)(smem + LY::flag_off) = 1;
         parity ^= 1u << s;
-        Slot v;
         {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
             const S *base = raw + L.yl*NX + L.xl;
             auto row = [&](int q, int b) -> const S * { return base + LY::off(q) + b*NX; };
@@ -314,16 +296,13 @@ struct TiledKernel {
                 a7 += y0w*ldv<S>(row(7, b)); a8 += y0w*ldv<S>(row(8, b));
                 a9 += y2w*ldv<S>(row(9, b)); a10 += y2w*ldv<S>(row(10, b));
             }
-            v.r34 = make_float2(a3, a4);
-            v.r1516 = make_float2(a15, a16);
-            v.r1718 = make_float2(a17, a18);
-            v.r56 = make_float2(ldv<S>(row(5, 0)), ldv<S>(row(6, 0)));
+            tmem_st8(tl + ring_col(p), a3, a4, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), a15, a16, a17, a18);
             const int o = L.yl*NX + L.xl;
             ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
         }
         __syncthreads();
-        // every thread has finished plane i-1: its stage can take plane i + NS - 1
-        if (p + LY::NS - 1 <= p1) issue(smem, (i + LY::NS - 1) % LY::NS, p + LY::NS - 1, y0, L, parity);
+        // every thread has finished plane i-1: its stage can take plane p + NS - 1
+        if (p + LY::NS - 1 <= P.p1) issue(smem, (i + LY::NS - 1) % LY::NS, p + LY::NS - 1, P, L, parity);
         {   // spanwise filter: two nodes of one row, five directions of one departure side
             const int m = NX - 1;
             const int x0 = L.xx0;
@@ -361,24 +340,31 @@ struct TiledKernel {
         __syncthreads();
         {
             const int o = L.yl*NX + L.xl, st = TY*NX;
-            v.r78 = make_float2(xbuf[0*st + o], xbuf[1*st + o]);
-            v.r910 = make_float2(xbuf[2*st + o], xbuf[3*st + o]);
-            v.r12 = make_float2(xbuf[4*st + o], xbuf[5*st + o]);
-            v.r1112 = make_float2(xbuf[6*st + o], xbuf[7*st + o]);
-            v.r1314 = make_float2(xbuf[8*st + o], xbuf[9*st + o]);
+            tmem_st8(tl + ring_col(p) + 8, xbuf[0*st + o], xbuf[2*st + o], xbuf[1*st + o], xbuf[3*st + o],
+                     xbuf[6*st + o], xbuf[8*st + o], xbuf[7*st + o], xbuf[9*st + o]);
+            tmem_st2(tl + r12_col(p), xbuf[4*st + o], xbuf[5*st + o]);
         }
-        return v;
     }
 
-    // a wall-cap target: xi weights and f0 from global memory, F1/F2 by direct gathers
-    __device__ __forceinline__ void cap_target(const Ring &R, int ph, int x, int y, int z, const Scal &sc, float &ub,
-                                               float &mass) const {
-        const size_t node = ((size_t)z*k.NY + y)*k.NX + x;
+    // Target t of tile row y, whose window (planes p-6 .. p) is complete in the ring. Staged
+    // targets take their xi weights and f0 row from the stage of plane p; the wall caps read them
+    // from global memory.
+    __device__ __forceinline__ void target(uint32_t tl, int p, int t, bool staged, const unsigned char *stage, int x,
+                                           int y, int yl, const Scal &sc, float &ub, float &mass) const {
+        constexpr int NX = LY::NX;
         float F[19];
-        xi_combine_phase(ph, R, T.wxi + ((size_t)z*k.NY + y)*64, F);
-        cap_f12(x, y, z, F);
-        F[0] = load_f<S>(fo, node, 0);
-        finish(F, x, y, z, sc, ub, mass);
+        tmem_wait_st();   // this thread's ring stores of plane p are complete
+        const float *wv = staged ? (const float *)(stage + LY::w_off) + yl*64 : T.wxi + ((size_t)t*k.NY + y)*64;
+        xi_combine(tl, p - 6, wv, F);
+        {
+            uint32_t r[2];
+            tmem_ld2(tl + r12_col(t), r);
+            tmem_wait_ld(r);
+            F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
+        }
+        if (staged) F[0] = ld1<S>((const S *)(stage + LY::f0_off) + yl*NX + x, (float)dev_ref(0));
+        else F[0] = load_f<S>(fo, ((size_t)t*k.NY + y)*NX + x, 0);
+        finish(F, x, y, t, sc, ub, mass);
     }
 
     __device__ __forceinline__ Lane lane() const {
@@ -405,41 +391,48 @@ struct TiledKernel {
         return sc;
     }
 
-    // One whole column (tile rows y0 .. y0+TY-1, all planes): returns its partial sums.
-    __device__ __forceinline__ void column(int tile, unsigned char *smem, Ring &R, unsigned &parity, bool &faulted,
-                                           const Lane &L, const Scal &sc, float &ub, float &mass) const {
-        constexpr int NX = LY::NX, TY = LY::TY;
+    // One piece of a column: planes P.p0 .. P.p1 through the ring; after plane p the targets
+    // whose window ends at p are completed (p = 6: the lower wall cap 0..3; p = NZ-1: targets
+    // NZ-4 .. NZ-1; otherwise target p-3). Adds the piece's partial sums to ub and mass.
+    __device__ __forceinline__ void piece(const Piece &P, unsigned char *smem, unsigned &parity, bool &faulted,
+                                          const Lane &L, uint32_t tl, const Scal &sc, float &ub, float &mass) const {
         const int NZ = k.NZ;
-        uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
-        const int y0 = tile*TY;
-        const int p1 = NZ - 1;
-        __syncthreads();   // every thread is done with every stage of the previous column
-        for (int s = 0; s < LY::NS - 1 && s <= p1; s++) issue(smem, s, s, y0, L, parity);
-        const int y = y0 + L.yl;
-        // planes 0..6 fill the ring (plane p in slot p mod 7); then the lower cap
+        __syncthreads();   // every thread is done with every stage of the previous piece
+        for (int s = 0; s < LY::NS - 1 && P.p0 + s <= P.p1; s++) issue(smem, s, P.p0 + s, P, L, parity);
+        const int y = P.y0 + L.yl;
 #pragma unroll 1
-        for (int p = 0; p < 7; p++) {
-            const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
-            ring_store(R, p, v);
+        for (int p = P.p0; p <= P.p1; p++) {
+            const int i = p - P.p0;
+            plane(i, p, P, smem, parity, faulted, L, tl);
+            if (i < 6) continue;   // window of plane p not yet in the ring
+            const unsigned char *stage = smem + (size_t)(i % LY::NS)*LY::stage_bytes;
+            const int lo = p == 6 ? 0 : p - 3, hi = p == NZ - 1 ? NZ - 1 : p - 3;
+            for (int t = max(lo, P.ta); t <= min(hi, P.tb - 1); t++)
+                target(tl, p, t, t == p - 3 && staged_target(p, P), stage, L.xl, y, L.yl, sc, ub, mass);
         }
-        for (int zt = 0; zt < 4; zt++) cap_target(R, 6, L.xl, y, zt, sc, ub, mass);
-        // steady state: each plane completes the window of one interior target
-        int ph = 0;   // slot of the newest plane = p mod 7
-#pragma unroll 1
-        for (int p = 7; p <= NZ - 1; p++) {
-            const Slot v = plane(p, p, p1, y0, smem, parity, faulted, L);
-            ring_store(R, ph, v);
-            const unsigned char *stage = smem + (size_t)(p % LY::NS)*LY::stage_bytes;
-            const float *wv = (const float *)(stage + LY::w_off) + L.yl*64;
-            float F[19];
-            xi_combine_phase(ph, R, wv, F);
-            F[0] = ld1<S>((const S *)(stage + LY::f0_off) + L.yl*NX + L.xl, (float)dev_ref(0));
-            finish(F, L.xl, y, p - 3, sc, ub, mass);
-            ph = ph == 6 ? 0 : ph + 1;
+    }
+
+    // TMEM ring: warp 0 allocates RING_COLS columns, every thread reads the base address
+    __device__ __forceinline__ uint32_t ring_alloc(unsigned char *smem, int tid) const {
+        uint32_t *slot = (uint32_t *)(smem + LY::flag_off + 8);
+        if (tid < 32) {
+            tmem_alloc(slot, RING_COLS);
+            tmem_relinquish();
         }
-        // upper cap: targets NZ-3 .. NZ-1 share the last window (newest plane NZ-1)
-        const int phl = (NZ - 1) % 7;
-        for (int zt = NZ - 3; zt < NZ; zt++) cap_target(R, phl, L.xl, y, zt, sc, ub, mass);
+        tmem_fence_before();
+        __syncthreads();
+        tmem_fence_after();
+        return *(volatile uint32_t *)slot + ((uint32_t)(32*((tid >> 5) & 3)) << 16);
+    }
+    __device__ __forceinline__ void ring_free(unsigned char *smem, int tid) const {
+        tmem_wait_ld();
+        tmem_wait_st();
+        tmem_fence_before();
+        __syncthreads();
+        if (tid < 32) {
+            tmem_fence_after();
+            tmem_dealloc(*(volatile uint32_t *)(smem + LY::flag_off + 8), RING_COLS);
+        }
     }
 
     __device__ void run() const {
@@ -451,22 +444,34 @@ struct TiledKernel {
             *(volatile int *)(smem + LY::flag_off) = 0;
             fence_mbar_init();
         }
-        __syncthreads();
+        const uint32_t tl = ring_alloc(smem, L.tid);   // includes the CTA barrier after the init
         unsigned parity = 0;   // bit s: parity of the next completion of stage s
         bool faulted = false;
         double ub_total = 0.0, mass_total = 0.0;
         const Scal sc = scalars();
-        Ring R;
-        // whole columns: CTA b takes tiles b, b + G, b + 2G, ... so that the CTAs running at the
-        // same time hold neighbouring tiles at similar heights and share the halo rows in L2
-        const int ntiles = k.NY/LY::TY;
-        for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-            float ub = 0.f, mass = 0.f;   // this column's partial sums
-            column(tile, smem, R, parity, faulted, L, sc, ub, mass);
+        // The (tile, target plane) sequence, tile-major, is cut into gridDim.x equal ranges; CTA b
+        // takes range b (one or more pieces of consecutive columns), so that every CTA has the
+        // same work and the CTAs running at the same time hold neighbouring tiles (halo rows
+        // shared through L2).
+        const int NZ = k.NZ;
+        const long long W = (long long)(k.NY/LY::TY)*NZ;
+        const long long lo = W*blockIdx.x/gridDim.x, hi = W*(blockIdx.x + 1)/gridDim.x;
+        for (long long u = lo; u < hi;) {
+            Piece P;
+            const int tile = (int)(u/NZ);
+            P.y0 = tile*LY::TY;
+            P.ta = (int)(u - (long long)tile*NZ);
+            P.tb = (int)min((long long)NZ, P.ta + (hi - u));
+            P.p0 = window_base(P.ta);
+            P.p1 = window_base(P.tb - 1) + 6;
+            float ub = 0.f, mass = 0.f;   // this piece's partial sums
+            piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
             ub_total += (double)ub;
             mass_total += (double)mass;
+            u += P.tb - P.ta;
         }
         drain(smem, parity, L.tid);
+        ring_free(smem, L.tid);
         end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0,
                               gridDim.x*gridDim.y*gridDim.z);
     }
@@ -485,10 +490,10 @@ struct BatchDesc {
 };
 
 template <class S, bool LES, int NXC>
-__global__ void __launch_bounds__(NTHREADS, 2) step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
+__global__ void __launch_bounds__(NTHREADS, 4) step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
 
 template <class S, bool LES, int NXC>
-__global__ void __launch_bounds__(NTHREADS, 2)
+__global__ void __launch_bounds__(NTHREADS, 4)
 step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const int2 *__restrict__ items, int nitems,
                         int macros_on) {
     using KT = TiledKernel<S, LES, NXC>;
@@ -504,6 +509,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         *(volatile int *)(smem + LY::flag_off) = 0;
         fence_mbar_init();
     }
+    const uint32_t tl = K.ring_alloc(smem, tid);   // uses no member of K
     unsigned parity = 0;
     bool faulted = false;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -527,14 +533,16 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         __syncthreads();
         const auto L = K.lane();
         const auto sc = K.scalars();
-        Ring R;
+        typename KT::Piece P;
+        P.y0 = w.y*LY::TY; P.ta = 0; P.tb = K.k.NZ; P.p0 = 0; P.p1 = K.k.NZ - 1;
         float ub = 0.f, mass = 0.f;
-        K.column(w.y, smem, R, parity, faulted, L, sc, ub, mass);
+        K.piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
         end_of_step<NTHREADS>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
                               (unsigned)descs[w.x].ntiles);
     }
     __syncthreads();
     if (nitems > 0) K.drain(smem, parity, tid);
+    K.ring_free(smem, tid);
 }
 
 template <class S, bool LES, int NXC>
@@ -630,7 +638,10 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     }
     const int tiles = k.NY/tc.TY;
     tc.units = (long long)tiles*k.NZ;
-    tc.grid = tiles < 2*num_sms ? tiles : 2*num_sms;   // two CTAs per SM
+    // persistent CTAs: as many as fit on the SMs by shared memory (228 KB per SM, 1 KB reserved
+    // per CTA), at most four (the register bound of the kernel and the TMEM ring's share)
+    const long long per_sm = std::min<long long>(4, (228*1024)/(tc.smem_bytes + 1024));
+    tc.grid = (int)std::min<long long>(tc.units, per_sm*num_sms);
     *out = tc;
     return tc.smem_bytes <= 227*1024 ? 0 : -1;
 }
