@@ -40,10 +40,13 @@ template <class S> constexpr int stages_for() { return 2; }
 
 // Shared-memory layout of one tile for a spanwise width NXC (a power of two): all offsets are
 // compile-time constants so every shared-memory address is a base plus an immediate.
-//   stage s (NS of them): population q in [1, 18] as `rows(q)` rows of NXC values
-//   (TY rows, or TY + 6 with the streamwise halo), then the target's xi weights (TY x 64
-//   floats) and f0 row (TY x NXC values); then ybuf [4][TY][NXC] and xbuf [10][TY][NXC] floats,
-//   then the stage mbarriers.
+//   front region (one): the populations read before the first barrier of a plane (the ten
+//     with e_y != 0 as TY + 6 rows with the streamwise halo, and 5, 6 as TY rows). All
+//     threads are done with it at that barrier, which is where the next plane's copies start,
+//     so one buffer overlaps the copies as well as two would;
+//   stage s (NS of them): populations 1, 2, 11..14 (TY rows each, read by the spanwise filter
+//     after that barrier), then the target's xi weights (TY x 64 floats) and f0 row;
+//   then ybuf [4][TY][NXC] and xbuf [10][TY][NXC] floats, then the stage mbarriers.
 template <class S, int NXC>
 struct Lay {
     static constexpr int NX = NXC;
@@ -52,24 +55,39 @@ struct Lay {
     static constexpr int EB = (int)sizeof(S);
     static constexpr int NS = stages_for<S>();
     static constexpr bool wide(int q) { return q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15; }
+    static constexpr bool front(int q) { return wide(q) || q == 5 || q == 6; }
     static constexpr int rows(int q) { return q == 0 ? 0 : (wide(q) ? TY + 6 : TY); }
     static constexpr int up16(int v) { return (v + 15)/16*16; }
+    // byte offset of population q within its region (front or stage)
     static constexpr int off_bytes(int q) {
         int off = 0;
-        for (int r = 1; r < q; ++r) off = up16(off + rows(r)*NX*EB);
+        for (int r = 1; r < q; ++r)
+            if (front(r) == front(q)) off = up16(off + rows(r)*NX*EB);
         return off;
     }
     static constexpr int off(int q) { return off_bytes(q)/EB; }
+    static constexpr int region_end(bool fr) {
+        int off = 0;
+        for (int r = 1; r < 19; ++r)
+            if (front(r) == fr) off = up16(off + rows(r)*NX*EB);
+        return off;
+    }
     static constexpr unsigned pops_bytes() {
         unsigned b = 0;
         for (int q = 1; q < 19; ++q) b += (unsigned)(rows(q)*NX*EB);
         return b;
     }
-    static constexpr int w_off = off_bytes(19);
+    static constexpr int front_bytes = (region_end(true) + 127)/128*128;
+    // front buffers: one for FP32 (four CTAs per SM fit); the 2-byte formats fit two, which keeps
+    // the next plane's copy from waiting for the slowest warp's streamwise filter
+    static constexpr int NF = EB == 2 ? 2 : 1;
+    static constexpr int front_off(int s) { return NF == 1 ? 0 : (s % NF)*front_bytes; }
+    static constexpr int w_off = region_end(false);   // within a stage
     static constexpr int f0_off = up16(w_off + TY*64*4);
     static constexpr int stage_bytes = (up16(f0_off + TY*NX*EB) + 127)/128*128;
+    static constexpr int stage_off(int s) { return NF*front_bytes + s*stage_bytes; }
     static constexpr unsigned tgt_bytes = (unsigned)(TY*64*4 + TY*NX*EB);
-    static constexpr int ybuf_off = NS*stage_bytes;
+    static constexpr int ybuf_off = NF*front_bytes + NS*stage_bytes;
     static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
     static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
     static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag, then the TMEM address
@@ -187,16 +205,16 @@ struct TiledKernel {
     // target's xi weights and f0 row). Jobs are spread over the four warps (job q on warp q & 3,
     // lane q >> 2) so that no warp serialises all the copy issues; thread 0 posts the expected
     // bytes (a copy may complete before that: the phase cannot end while the arrival is due).
-    __device__ void issue_plane(unsigned char *stage, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
+    __device__ void issue_plane(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int NY = k.NY, NZ = k.NZ;
         const size_t N = (size_t)NX*NY*NZ;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
         if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
-        S *pops = (S *)stage;
+        unsigned char *stage = smem + LY::stage_off(s);
         const int q = 4*(tid & 31) + (tid >> 5);   // lanes 0..5 only
         if (q >= 1 && q < 19) {
-            S *dst = pops + LY::off(q);
+            S *dst = (S *)(LY::front(q) ? smem + LY::front_off(s) : stage) + LY::off(q);
             const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
             if (!LY::wide(q)) {
                 bulk_g2s(dst, plane_base + (size_t)y0*NX, TY*row_bytes, bar);
@@ -263,8 +281,7 @@ struct TiledKernel {
         if (*(volatile int *)(smem + LY::flag_off)) return;
         if (p == k.drill_plane) return;   // failure drill: this plane's copies never start
         fence_proxy_async();
-        issue_plane(smem + (size_t)s*LY::stage_bytes, (uint64_t *)(smem + LY::bar_off) + s, p, P.y0, staged_target(p, P),
-                    L.tid);
+        issue_plane(smem, s, (uint64_t *)(smem + LY::bar_off) + s, p, P.y0, staged_target(p, P), L.tid);
         if (L.tid == 0)
             parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
     }
@@ -278,27 +295,31 @@ struct TiledKernel {
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         float *ybuf = (float *)(smem + LY::ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
         float *xbuf = (float *)(smem + LY::xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
-        unsigned char *stage = smem + (size_t)s*LY::stage_bytes;
-        const S *raw = (const S *)stage;
+        const S *raw = (const S *)(smem + LY::stage_off(s));   // populations 1, 2, 11..14
+        const S *frontp = (const S *)(smem + LY::front_off(s));  // populations read before the barrier
         if (mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted)) parity &= ~(1u << (PEND + s));
         else if (faulted) *(volatile int *)(smem + LY::flag_off) = 1;
         parity ^= 1u << s;
         {   // streamwise filter over rows yl .. yl+6 of the halo copy, and raw values of 5, 6
-            const S *base = raw + L.yl*NX + L.xl;
+            const S *base = frontp + L.yl*NX + L.xl;
             auto row = [&](int q, int b) -> const S * { return base + LY::off(q) + b*NX; };
-            float a3 = 0, a4 = 0, a15 = 0, a16 = 0, a17 = 0, a18 = 0, a7 = 0, a8 = 0, a9 = 0, a10 = 0;
+            // packed pairs: the first of each pair departs from y - minSize (weights wy0), the
+            // second from y + minSize (wy2)
+            P2 a34 = p2(0.f, 0.f), a1516 = a34, a1718 = a34, a79 = a34, a810 = a34;
 #pragma unroll
             for (int b = 0; b < 7; b++) {
-                const float y0w = tc.wy0[b], y2w = tc.wy2[b];
-                a3 += y0w*ldv<S>(row(3, b)); a4 += y2w*ldv<S>(row(4, b));
-                a15 += y0w*ldv<S>(row(15, b)); a16 += y2w*ldv<S>(row(16, b));
-                a17 += y0w*ldv<S>(row(17, b)); a18 += y2w*ldv<S>(row(18, b));
-                a7 += y0w*ldv<S>(row(7, b)); a8 += y0w*ldv<S>(row(8, b));
-                a9 += y2w*ldv<S>(row(9, b)); a10 += y2w*ldv<S>(row(10, b));
+                const P2 w = p2(tc.wy0[b], tc.wy2[b]);
+                fma2(a34, w, p2(ldv<S>(row(3, b)), ldv<S>(row(4, b))));
+                fma2(a1516, w, p2(ldv<S>(row(15, b)), ldv<S>(row(16, b))));
+                fma2(a1718, w, p2(ldv<S>(row(17, b)), ldv<S>(row(18, b))));
+                fma2(a79, w, p2(ldv<S>(row(7, b)), ldv<S>(row(9, b))));
+                fma2(a810, w, p2(ldv<S>(row(8, b)), ldv<S>(row(10, b))));
             }
-            tmem_st8(tl + ring_col(p), a3, a4, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), a15, a16, a17, a18);
+            const float2 v34 = unp(a34), v1516 = unp(a1516), v1718 = unp(a1718), v79 = unp(a79), v810 = unp(a810);
+            tmem_st8(tl + ring_col(p), v34.x, v34.y, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), v1516.x, v1516.y, v1718.x,
+                     v1718.y);
             const int o = L.yl*NX + L.xl;
-            ybuf[0*TY*NX + o] = a7; ybuf[1*TY*NX + o] = a8; ybuf[2*TY*NX + o] = a9; ybuf[3*TY*NX + o] = a10;
+            ybuf[0*TY*NX + o] = v79.x; ybuf[1*TY*NX + o] = v810.x; ybuf[2*TY*NX + o] = v79.y; ybuf[3*TY*NX + o] = v810.y;
         }
         __syncthreads();
         // every thread has finished plane i-1: its stage can take plane p + NS - 1
@@ -405,7 +426,7 @@ struct TiledKernel {
             const int i = p - P.p0;
             plane(i, p, P, smem, parity, faulted, L, tl);
             if (i < 6) continue;   // window of plane p not yet in the ring
-            const unsigned char *stage = smem + (size_t)(i % LY::NS)*LY::stage_bytes;
+            const unsigned char *stage = smem + LY::stage_off(i % LY::NS);
             const int lo = p == 6 ? 0 : p - 3, hi = p == NZ - 1 ? NZ - 1 : p - 3;
             for (int t = max(lo, P.ta); t <= min(hi, P.tb - 1); t++)
                 target(tl, p, t, t == p - 3 && staged_target(p, P), stage, L.xl, y, L.yl, sc, ub, mass);
@@ -588,8 +609,6 @@ size_t smem_for(int nx) {
     return nx == 32 ? Lay<S, 32>::smem_bytes : (nx == 64 ? Lay<S, 64>::smem_bytes : Lay<S, 128>::smem_bytes);
 }
 
-size_t elem_bytes(int precision) { return precision == ISLBM_FP32 ? 4 : 2; }
-
 }  // namespace
 
 bool tiled_supported(const StepConst &k, int precision) {
@@ -609,28 +628,6 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     int l = 0;
     while ((1 << l) < k.NX) l++;
     tc.log2nx = l;
-    const size_t eb = elem_bytes(precision);
-    auto up16 = [](size_t v) { return (v + 15)/16*16; };
-    size_t off = 0;   // bytes within a stage
-    tc.off[0] = 0; tc.rows[0] = 0;
-    size_t used = 0;
-    for (int q = 1; q < 19; q++) {
-        const bool wide = (q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15);
-        tc.rows[q] = wide ? tc.TY + 6 : tc.TY;
-        tc.off[q] = (int)(off/eb);
-        off = up16(off + (size_t)tc.rows[q]*k.NX*eb);
-        used += (size_t)tc.rows[q]*k.NX*eb;
-    }
-    tc.stage_bytes_used = (unsigned)used;
-    tc.w_off = (unsigned)off;
-    off = up16(off + (size_t)tc.TY*64*sizeof(float));
-    tc.f0_off = (unsigned)off;
-    off = up16(off + (size_t)tc.TY*k.NX*eb);
-    tc.tgt_bytes = (unsigned)(tc.TY*64*sizeof(float) + tc.TY*k.NX*eb);
-    tc.stage_bytes = (off + 127)/128*128;
-    tc.ybuf_off = 2*tc.stage_bytes;
-    tc.xbuf_off = tc.ybuf_off + (size_t)4*tc.TY*k.NX*sizeof(float);
-    tc.bar_off = tc.xbuf_off + (size_t)10*tc.TY*k.NX*sizeof(float);
     tc.smem_bytes = precision == ISLBM_FP32 ? smem_for<float>(k.NX) : smem_for<__half>(k.NX);
     for (int a = 0; a < 7; a++) {
         tc.wx0[a] = (float)wx0[a]; tc.wx2[a] = (float)wx2[a];

@@ -14,12 +14,7 @@ struct TiledConst {
     int grid;                     // persistent CTAs
     long long units;              // tiles * NZ (flattened work)
     int log2nx;
-    int off[19];                  // element offset of each population's region within a stage
-    int rows[19];                 // rows staged per population (TY, or TY + 6 with the halo)
-    size_t stage_bytes, smem_bytes, ybuf_off, xbuf_off, bar_off;
-    unsigned stage_bytes_used;    // bytes the population copies of one plane deliver
-    unsigned w_off, f0_off;       // byte offsets of the target's xi weights and f0 row in a stage
-    unsigned tgt_bytes;           // bytes of those two copies
+    size_t smem_bytes;            // dynamic shared memory per CTA (layout: Lay in step_tiled.cu)
     float wx0[7], wx2[7], wy0[7], wy2[7];   // uniform-spacing Lagrange weights
     unsigned long long n;         // step number (set per launch)
 };
