@@ -98,16 +98,17 @@ struct Lay {
 // xi ring in tensor memory: each thread keeps the filtered values of the 7 planes of its
 // current window in its own TMEM lane; plane p sits in slot p mod 7:
 //   columns 16*s .. 16*s+15: pairs (3,4) (5,6) (15,16) (17,18) (7,9) (8,10) (11,13) (12,14),
-//   columns 112 + 2*s, +1: the spanwise-filtered F1, F2 of the plane (used by target p).
+//   columns 112 + 2*(p mod 8), +1: the spanwise-filtered F1, F2 of plane p (used by target p,
+//   which completes at most three planes later).
 // The pairs are chosen so that each pair's xi weights are adjacent in the weight row.
 constexpr int RING_COLS = 128;   // TMEM columns per CTA (power of two >= 32)
-__device__ __forceinline__ int ring_col(int p) { return 16*(p % 7); }
-__device__ __forceinline__ int r12_col(int p) { return 112 + 2*(p % 7); }
+__device__ __forceinline__ int ring_col(int slot) { return 16*slot; }   // slot = p mod 7, tracked by the caller
+__device__ __forceinline__ int r12_col(int p) { return 112 + 2*(p & 7); }
 
 // xi combination of the window of planes b .. b+6 held in the TMEM ring (`tl` = this warp's
-// lane-quarter address). The 64 weights of (y, z) are interleaved per stencil point c:
+// lane-quarter address, `sb` = b mod 7). The 64 weights of (y, z) are interleaved per stencil point c:
 // (xi3, xi4, xi5, xi6, xi15, xi16, xi17, xi18)[c]. Writes F[3..18].
-__device__ __forceinline__ void xi_combine(uint32_t tl, int b, const float *wv_, float *F) {
+__device__ __forceinline__ void xi_combine(uint32_t tl, int sb, const float *wv_, float *F) {
     const float4 *wv = (const float4 *)wv_;
     P2 a34 = p2(0.f, 0.f), a56 = a34, a1516 = a34, a1718 = a34, a79 = a34, a810 = a34, a1113 = a34, a1214 = a34;
     auto acc = [&](const uint32_t (&q)[16], int c) {
@@ -125,15 +126,16 @@ __device__ __forceinline__ void xi_combine(uint32_t tl, int b, const float *wv_,
 #pragma unroll
     for (int c = 0; c < 6; c += 2) {
         uint32_t q0[16], q1[16];
-        tmem_ld16(tl + ring_col(b + c), q0);
-        tmem_ld16(tl + ring_col(b + c + 1), q1);
+        const int s0 = sb + c, s1 = sb + c + 1;
+        tmem_ld16(tl + ring_col(s0 >= 7 ? s0 - 7 : s0), q0);
+        tmem_ld16(tl + ring_col(s1 >= 7 ? s1 - 7 : s1), q1);
         tmem_wait_ld(q0, q1);
         acc(q0, c);
         acc(q1, c + 1);
     }
     {
         uint32_t q0[16];
-        tmem_ld16(tl + ring_col(b + 6), q0);
+        tmem_ld16(tl + ring_col(sb == 0 ? 6 : sb - 1), q0);
         tmem_wait_ld(q0);
         acc(q0, 6);
     }
@@ -289,7 +291,7 @@ struct TiledKernel {
     // One source plane (the i-th of its piece): wait for its copies, filter, and store the
     // plane's values in the TMEM ring slot of plane p.
     __device__ __forceinline__ void plane(int i, int p, const Piece &P, unsigned char *smem, unsigned &parity,
-                                          bool &faulted, const Lane &L, uint32_t tl) const {
+                                          bool &faulted, const Lane &L, uint32_t tl, int sp) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int s = i % LY::NS;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
@@ -316,7 +318,7 @@ struct TiledKernel {
                 fma2(a810, w, p2(ldv<S>(row(8, b)), ldv<S>(row(10, b))));
             }
             const float2 v34 = unp(a34), v1516 = unp(a1516), v1718 = unp(a1718), v79 = unp(a79), v810 = unp(a810);
-            tmem_st8(tl + ring_col(p), v34.x, v34.y, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), v1516.x, v1516.y, v1718.x,
+            tmem_st8(tl + ring_col(sp), v34.x, v34.y, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), v1516.x, v1516.y, v1718.x,
                      v1718.y);
             const int o = L.yl*NX + L.xl;
             ybuf[0*TY*NX + o] = v79.x; ybuf[1*TY*NX + o] = v810.x; ybuf[2*TY*NX + o] = v79.y; ybuf[3*TY*NX + o] = v810.y;
@@ -361,7 +363,7 @@ struct TiledKernel {
         __syncthreads();
         {
             const int o = L.yl*NX + L.xl, st = TY*NX;
-            tmem_st8(tl + ring_col(p) + 8, xbuf[0*st + o], xbuf[2*st + o], xbuf[1*st + o], xbuf[3*st + o],
+            tmem_st8(tl + ring_col(sp) + 8, xbuf[0*st + o], xbuf[2*st + o], xbuf[1*st + o], xbuf[3*st + o],
                      xbuf[6*st + o], xbuf[8*st + o], xbuf[7*st + o], xbuf[9*st + o]);
             tmem_st2(tl + r12_col(p), xbuf[4*st + o], xbuf[5*st + o]);
         }
@@ -370,13 +372,16 @@ struct TiledKernel {
     // Target t of tile row y, whose window (planes p-6 .. p) is complete in the ring. Staged
     // targets take their xi weights and f0 row from the stage of plane p; the wall caps read them
     // from global memory.
-    __device__ __forceinline__ void target(uint32_t tl, int p, int t, bool staged, const unsigned char *stage, int x,
+    __device__ __forceinline__ void target(uint32_t tl, int sp, int t, bool staged, const unsigned char *stage, int x,
                                            int y, int yl, const Scal &sc, float &ub, float &mass) const {
         constexpr int NX = LY::NX;
         float F[19];
         tmem_wait_st();   // this thread's ring stores of plane p are complete
-        const float *wv = staged ? (const float *)(stage + LY::w_off) + yl*64 : T.wxi + ((size_t)t*k.NY + y)*64;
-        xi_combine(tl, p - 6, wv, F);
+        // window base p - 6 sits in slot (sp + 1) mod 7; separate calls keep each weight pointer
+        // in its own address space (shared or global)
+        const int sb = sp == 6 ? 0 : sp + 1;
+        if (staged) xi_combine(tl, sb, (const float *)(stage + LY::w_off) + yl*64, F);
+        else xi_combine(tl, sb, T.wxi + ((size_t)t*k.NY + y)*64, F);
         {
             uint32_t r[2];
             tmem_ld2(tl + r12_col(t), r);
@@ -421,15 +426,16 @@ struct TiledKernel {
         __syncthreads();   // every thread is done with every stage of the previous piece
         for (int s = 0; s < LY::NS - 1 && P.p0 + s <= P.p1; s++) issue(smem, s, P.p0 + s, P, L, parity);
         const int y = P.y0 + L.yl;
+        int sp = P.p0 % 7;   // ring slot of plane p
 #pragma unroll 1
-        for (int p = P.p0; p <= P.p1; p++) {
+        for (int p = P.p0; p <= P.p1; p++, sp = sp == 6 ? 0 : sp + 1) {
             const int i = p - P.p0;
-            plane(i, p, P, smem, parity, faulted, L, tl);
+            plane(i, p, P, smem, parity, faulted, L, tl, sp);
             if (i < 6) continue;   // window of plane p not yet in the ring
             const unsigned char *stage = smem + LY::stage_off(i % LY::NS);
             const int lo = p == 6 ? 0 : p - 3, hi = p == NZ - 1 ? NZ - 1 : p - 3;
             for (int t = max(lo, P.ta); t <= min(hi, P.tb - 1); t++)
-                target(tl, p, t, t == p - 3 && staged_target(p, P), stage, L.xl, y, L.yl, sc, ub, mass);
+                target(tl, sp, t, t == p - 3 && staged_target(p, P), stage, L.xl, y, L.yl, sc, ub, mass);
         }
     }
 
