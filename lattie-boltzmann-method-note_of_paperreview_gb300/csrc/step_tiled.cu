@@ -476,26 +476,25 @@ struct TiledKernel {
         bool faulted = false;
         double ub_total = 0.0, mass_total = 0.0;
         const Scal sc = scalars();
-        // The (tile, target plane) sequence, tile-major, is cut into gridDim.x equal ranges; CTA b
-        // takes range b (one or more pieces of consecutive columns), so that every CTA has the
-        // same work and the CTAs running at the same time hold neighbouring tiles (halo rows
-        // shared through L2).
+        // Work items: each column is cut into tc.zsegs equal wall-normal segments; item
+        // (segment s, tile) = s*ntiles + tile. CTAs take items b, b + G, ..., so the CTAs
+        // running at the same time hold neighbouring tiles of the same segment and reach the
+        // same plane at about the same time: the streamwise halo rows each CTA copies are the
+        // neighbours' own rows, read from HBM once and from L2 by the others.
         const int NZ = k.NZ;
-        const long long W = (long long)(k.NY/LY::TY)*NZ;
-        const long long lo = W*blockIdx.x/gridDim.x, hi = W*(blockIdx.x + 1)/gridDim.x;
-        for (long long u = lo; u < hi;) {
+        const int ntiles = k.NY/LY::TY, nseg = tc.zsegs;
+        for (int item = blockIdx.x; item < ntiles*nseg; item += gridDim.x) {
+            const int tile = item % ntiles, seg = item/ntiles;
             Piece P;
-            const int tile = (int)(u/NZ);
             P.y0 = tile*LY::TY;
-            P.ta = (int)(u - (long long)tile*NZ);
-            P.tb = (int)min((long long)NZ, P.ta + (hi - u));
+            P.ta = seg*NZ/nseg;
+            P.tb = (seg + 1)*NZ/nseg;
             P.p0 = window_base(P.ta);
             P.p1 = window_base(P.tb - 1) + 6;
             float ub = 0.f, mass = 0.f;   // this piece's partial sums
             piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
             ub_total += (double)ub;
             mass_total += (double)mass;
-            u += P.tb - P.ta;
         }
         drain(smem, parity, L.tid);
         ring_free(smem, L.tid);
@@ -643,8 +642,12 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     tc.units = (long long)tiles*k.NZ;
     // persistent CTAs: as many as fit on the SMs by shared memory (228 KB per SM, 1 KB reserved
     // per CTA), at most four (the register bound of the kernel and the TMEM ring's share)
-    const long long per_sm = std::min<long long>(4, (228*1024)/(tc.smem_bytes + 1024));
-    tc.grid = (int)std::min<long long>(tc.units, per_sm*num_sms);
+    const int per_sm = (int)std::min<size_t>(4, (228*1024)/(tc.smem_bytes + 1024));
+    const int slots = per_sm*num_sms;
+    // wall-normal segments per column: enough items to fill the resident slots, each at
+    // least 16 targets long (a segment re-reads the 6 planes below it to fill its ring)
+    tc.zsegs = std::max(1, std::min(slots/tiles, k.NZ/16));
+    tc.grid = std::min(tiles*tc.zsegs, slots);
     *out = tc;
     return tc.smem_bytes <= 227*1024 ? 0 : -1;
 }

@@ -12,6 +12,7 @@ namespace islbm {
 struct TiledConst {
     int TY;                       // streamwise rows per tile (256 / NX)
     int grid;                     // persistent CTAs
+    int zsegs;                    // wall-normal segments per column (work items = tiles * zsegs)
     long long units;              // tiles * NZ (flattened work)
     int log2nx;
     size_t smem_bytes;            // dynamic shared memory per CTA (layout: Lay in step_tiled.cu)
