@@ -203,38 +203,62 @@ struct TiledKernel {
         if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
     }
 
-    // Copy job q of a plane (1..18: population q, two pieces when the halo wraps; 19, 20: the
+    // Copy jobs of a plane (1..18: population q, two pieces when the halo wraps; 19, 20: the
     // target's xi weights and f0 row). Jobs are spread over the four warps (job q on warp q & 3,
     // lane q >> 2) so that no warp serialises all the copy issues; thread 0 posts the expected
     // bytes (a copy may complete before that: the phase cannot end while the arrival is due).
-    __device__ void issue_plane(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
+    // Copy job Q (compile-time) of plane p into stage s.
+    template <int Q>
+    __device__ __forceinline__ void copy_job(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt) const {
         constexpr int NX = LY::NX, TY = LY::TY;
-        const int NY = k.NY, NZ = k.NZ;
-        const size_t N = (size_t)NX*NY*NZ;
+        const int NY = k.NY;
         const unsigned row_bytes = (unsigned)(NX*sizeof(S));
-        if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         unsigned char *stage = smem + LY::stage_off(s);
-        const int q = 4*(tid & 31) + (tid >> 5);   // lanes 0..5 only
-        if (q >= 1 && q < 19) {
-            S *dst = (S *)(LY::front(q) ? smem + LY::front_off(s) : stage) + LY::off(q);
-            const S *plane_base = fo + (size_t)q*N + (size_t)p*NY*NX;
-            if (!LY::wide(q)) {
+        if constexpr (Q < 19) {
+            const size_t N = (size_t)NX*NY*k.NZ;
+            S *dst = (S *)(LY::front(Q) ? smem + LY::front_off(s) : stage) + LY::off(Q);
+            const S *plane_base = fo + (size_t)Q*N + (size_t)p*NY*NX;
+            if constexpr (!LY::wide(Q)) {
                 bulk_g2s(dst, plane_base + (size_t)y0*NX, TY*row_bytes, bar);
             } else {
                 const int ys = y0 >= 3 ? y0 - 3 : y0 - 3 + NY;
-                const int rows = TY + 6;
+                constexpr int rows = TY + 6;
                 const int first = min(rows, NY - ys);
                 bulk_g2s(dst, plane_base + (size_t)ys*NX, first*row_bytes, bar);
                 if (first < rows) bulk_g2s(dst + (size_t)first*NX, plane_base, (rows - first)*row_bytes, bar);
             }
+        } else if constexpr (Q == 19) {
+            if (tgt) bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)(p - 3)*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
+        } else {
+            if (tgt) bulk_g2s(stage + LY::f0_off, fo + ((size_t)(p - 3)*NY + y0)*NX, TY*row_bytes, bar);
         }
-        if (tgt && q == 19) {
-            const int z = p - 3;
-            bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)z*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
-        }
-        if (tgt && q == 20) {
-            const int z = p - 3;
-            bulk_g2s(stage + LY::f0_off, fo + ((size_t)z*NY + y0)*NX, TY*row_bytes, bar);
+    }
+
+    __device__ void issue_plane(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
+        if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
+        // job q = 4*lane + warp (lanes 0..5), dispatched to compile-time job bodies
+        switch (4*(tid & 31) + (tid >> 5)) {
+        case 1: copy_job<1>(smem, s, bar, p, y0, tgt); break;
+        case 2: copy_job<2>(smem, s, bar, p, y0, tgt); break;
+        case 3: copy_job<3>(smem, s, bar, p, y0, tgt); break;
+        case 4: copy_job<4>(smem, s, bar, p, y0, tgt); break;
+        case 5: copy_job<5>(smem, s, bar, p, y0, tgt); break;
+        case 6: copy_job<6>(smem, s, bar, p, y0, tgt); break;
+        case 7: copy_job<7>(smem, s, bar, p, y0, tgt); break;
+        case 8: copy_job<8>(smem, s, bar, p, y0, tgt); break;
+        case 9: copy_job<9>(smem, s, bar, p, y0, tgt); break;
+        case 10: copy_job<10>(smem, s, bar, p, y0, tgt); break;
+        case 11: copy_job<11>(smem, s, bar, p, y0, tgt); break;
+        case 12: copy_job<12>(smem, s, bar, p, y0, tgt); break;
+        case 13: copy_job<13>(smem, s, bar, p, y0, tgt); break;
+        case 14: copy_job<14>(smem, s, bar, p, y0, tgt); break;
+        case 15: copy_job<15>(smem, s, bar, p, y0, tgt); break;
+        case 16: copy_job<16>(smem, s, bar, p, y0, tgt); break;
+        case 17: copy_job<17>(smem, s, bar, p, y0, tgt); break;
+        case 18: copy_job<18>(smem, s, bar, p, y0, tgt); break;
+        case 19: copy_job<19>(smem, s, bar, p, y0, tgt); break;
+        case 20: copy_job<20>(smem, s, bar, p, y0, tgt); break;
+        default: break;
         }
     }
 
