@@ -2,22 +2,23 @@
 //
 // Same step as stream_collide (C/evolution.h:358-684) for FP32 arithmetic with FP32, FP16 or
 // BF16 population storage, organised for HBM:
-//   * a CTA owns a tile of TY = 128/NX full-width rows (all NX spanwise nodes) and marches
-//     upward through the wall-normal planes of that column; every plane of the 18 moving
-//     populations is copied global -> shared with cp.async.bulk (one copy per population and
-//     plane, 3-row streamwise halo for the ten populations with e_y != 0, periodic wrap by
-//     splitting the copy), tracked by an mbarrier, 2 stages deep; the target plane's xi
-//     weights and f0 row ride in the same stage;
+//   * a CTA owns a tile of TY = 128/NX full-width rows (all NX spanwise nodes), one node per
+//     thread, and marches upward through a segment of the wall-normal planes of that column;
+//     every plane of the 18 moving populations is copied global -> shared with cp.async.bulk
+//     (one copy per population and plane, 3-row streamwise halo for the ten populations with
+//     e_y != 0, periodic wrap by splitting the copy), tracked by an mbarrier per stage; the
+//     target plane's xi weights and f0 row ride in the same stage;
 //   * the interpolation is applied as separable filters, exact in real arithmetic because the
 //     x and y weights are the same for every node (uniform spacing, C/initialization.h:51-108)
 //     and the xi weights depend only on the target (y, z): a streamwise filter over the halo
-//     rows, then a spanwise filter (2 nodes per task) through shared memory, then the xi
-//     combination over a 7-plane ring of filtered values kept in registers (packed FP32x2
-//     FMAs), so each loaded value feeds 7 target planes without being re-read;
+//     rows, a spanwise filter of each node over its row (streamwise-filtered values exchanged
+//     through shared memory), then the xi combination over a 7-plane ring of filtered values
+//     kept in tensor memory (TMEM, one lane per thread), all in packed FP32x2 FMAs, so each
+//     loaded value feeds 7 target planes without being re-read;
 //   * the collision tail, wall bounce-back, BFL rows and controller partial sums are fused;
-//   * CTAs are persistent (2 per SM, 128 threads each) and take whole columns: CTA b takes
-//     tiles b, b + G, b + 2G, ..., so CTAs running at the same time hold neighbouring tiles at
-//     similar heights and share the streamwise halo rows through L2.
+//   * CTAs are persistent (up to 4 per SM, 128 threads each); work items are (segment, tile)
+//     pairs taken segment-major, so the CTAs running at the same time hold neighbouring tiles
+//     at similar heights and share the streamwise halo rows through L2.
 // Every value of the old populations is read from HBM about once per step (halo rows come
 // from L2); every new value is written once.
 #include <algorithm>
@@ -46,7 +47,8 @@ template <class S> constexpr int stages_for() { return 2; }
 //     so one buffer overlaps the copies as well as two would;
 //   stage s (NS of them): populations 1, 2, 11..14 (TY rows each, read by the spanwise filter
 //     after that barrier), then the target's xi weights (TY x 64 floats) and f0 row;
-//   then ybuf [4][TY][NXC] and xbuf [10][TY][NXC] floats, then the stage mbarriers.
+//   then ybuf [2][TY][NXC] float4 (streamwise-filtered 7, 8, 9, 10 of each node, two buffers
+//   by plane parity), then the stage mbarriers.
 template <class S, int NXC>
 struct Lay {
     static constexpr int NX = NXC;
@@ -88,8 +90,7 @@ struct Lay {
     static constexpr int stage_off(int s) { return NF*front_bytes + s*stage_bytes; }
     static constexpr unsigned tgt_bytes = (unsigned)(TY*64*4 + TY*NX*EB);
     static constexpr int ybuf_off = NF*front_bytes + NS*stage_bytes;
-    static constexpr int xbuf_off = ybuf_off + 4*TY*NX*4;
-    static constexpr int bar_off = xbuf_off + 10*TY*NX*4;
+    static constexpr int bar_off = ybuf_off + 2*TY*NX*16;
     static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag, then the TMEM address
     // at least 46 KB, so that no more than four CTAs (4 x RING_COLS TMEM columns) share an SM
     static constexpr int smem_bytes = flag_off + 16 > 46*1024 ? flag_off + 16 : 46*1024;
@@ -187,7 +188,15 @@ struct TiledKernel {
         }
         if (z <= 1) {
             const int nb = 2*k.NYD6, r = z*k.NYD6 + (y + 3);
-            if (T.bfl_flag[r] | T.bfl_flag[nb + r] | T.bfl_flag[2*nb + r] | T.bfl_flag[3*nb + r]) bfl_node<S>(fo, T, k, x, y, z, F);
+            if (T.bfl_flag[r] | T.bfl_flag[nb + r] | T.bfl_flag[2*nb + r] | T.bfl_flag[3*nb + r]) {
+                // the out-of-line BFL rows work on a copy, so that F itself never needs an address
+                float G[19];
+#pragma unroll
+                for (int q = 0; q < 19; q++) G[q] = F[q];
+                bfl_node<S>(fo, T, k, x, y, z, G);
+#pragma unroll
+                for (int q = 0; q < 19; q++) F[q] = G[q];
+            }
         }
         float Fl[19];
 #pragma unroll
@@ -279,8 +288,6 @@ struct TiledKernel {
 
     struct Lane {
         int tid, xl, yl;        // node of this thread within the tile
-        int xr, xx0;            // spanwise-filter task: row and first of two nodes
-        int xsel;               // 0: departure x - minSize (7, 9, 1, 11, 13), 1: x + minSize
     };
 
     // A piece of a column: targets ta .. tb-1 of tile rows y0 .. y0+TY-1, computed from source
@@ -319,8 +326,7 @@ struct TiledKernel {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int s = i % LY::NS;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
-        float *ybuf = (float *)(smem + LY::ybuf_off);   // [4][TY][NX]  dirs 7, 8, 9, 10
-        float *xbuf = (float *)(smem + LY::xbuf_off);   // [10][TY][NX] dirs 7..10, 1, 2, 11..14
+        float4 *ybuf = (float4 *)(smem + LY::ybuf_off) + (i & 1)*TY*NX + L.yl*NX;   // this row, this plane
         const S *raw = (const S *)(smem + LY::stage_off(s));   // populations 1, 2, 11..14
         const S *frontp = (const S *)(smem + LY::front_off(s));  // populations read before the barrier
         if (mbar_wait(&bars[s], (parity >> s) & 1u, ctrl, faulted)) parity &= ~(1u << (PEND + s));
@@ -344,52 +350,29 @@ struct TiledKernel {
             const float2 v34 = unp(a34), v1516 = unp(a1516), v1718 = unp(a1718), v79 = unp(a79), v810 = unp(a810);
             tmem_st8(tl + ring_col(sp), v34.x, v34.y, ldv<S>(row(5, 0)), ldv<S>(row(6, 0)), v1516.x, v1516.y, v1718.x,
                      v1718.y);
-            const int o = L.yl*NX + L.xl;
-            ybuf[0*TY*NX + o] = v79.x; ybuf[1*TY*NX + o] = v810.x; ybuf[2*TY*NX + o] = v79.y; ybuf[3*TY*NX + o] = v810.y;
+            ybuf[L.xl] = make_float4(v79.x, v810.x, v79.y, v810.y);   // 7, 8, 9, 10
         }
         __syncthreads();
         // every thread has finished plane i-1: its stage can take plane p + NS - 1
         if (p + LY::NS - 1 <= P.p1) issue(smem, (i + LY::NS - 1) % LY::NS, p + LY::NS - 1, P, L, parity);
-        {   // spanwise filter: two nodes of one row, five directions of one departure side
-            const int m = NX - 1;
-            const int x0 = L.xx0;
-            const int xa = (x0 - 4) & m, xb = (x0 - 2) & m, xc = x0, xd = (x0 + 2) & m, xe = (x0 + 4) & m;
-            auto task = [&](auto jc) {
-                constexpr int j = decltype(jc)::value;
-                const int d = 2*j + L.xsel;        // xbuf slot: 7, 8, 9, 10, 1, 2, 11, 12, 13, 14
-                float vv[10];
-                if constexpr (j < 2) {
-                    const float *in = ybuf + (size_t)d*TY*NX + L.xr*NX;
-                    const float2 a = *(const float2 *)(in + xa), b = *(const float2 *)(in + xb), c = *(const float2 *)(in + xc),
-                                 e = *(const float2 *)(in + xd), g = *(const float2 *)(in + xe);
-                    vv[0] = a.x; vv[1] = a.y; vv[2] = b.x; vv[3] = b.y; vv[4] = c.x; vv[5] = c.y; vv[6] = e.x; vv[7] = e.y; vv[8] = g.x; vv[9] = g.y;
-                } else {
-                    // population of this task: 1, 11, 13 (xsel 0) or 2, 12, 14 (xsel 1)
-                    constexpr int qa = j == 2 ? 1 : (j == 3 ? 11 : 13);
-                    constexpr int qb = j == 2 ? 2 : (j == 3 ? 12 : 14);
-                    const S *in = raw + (L.xsel ? LY::off(qb) : LY::off(qa)) + L.xr*NX;
-                    const float2 a = ldv2<S>(in + xa), b = ldv2<S>(in + xb), c = ldv2<S>(in + xc), e = ldv2<S>(in + xd),
-                                 g = ldv2<S>(in + xe);
-                    vv[0] = a.x; vv[1] = a.y; vv[2] = b.x; vv[3] = b.y; vv[4] = c.x; vv[5] = c.y; vv[6] = e.x; vv[7] = e.y; vv[8] = g.x; vv[9] = g.y;
-                }
-                float o0 = 0, o1 = 0;
+        {   // spanwise filter of this thread's node: x - minSize (wx0) for 7, 9, 1, 11, 13 and
+            // x + minSize (wx2) for 8, 10, 2, 12, 14, packed as pairs
+            const S *raw_row = raw + L.yl*NX;
+            P2 a78 = p2(0.f, 0.f), a910 = a78, a12 = a78, a1112 = a78, a1314 = a78;
 #pragma unroll
-                for (int a = 0; a < 7; a++) {
-                    const float w = L.xsel ? tc.wx2[a] : tc.wx0[a];
-                    o0 += w*vv[a + 1]; o1 += w*vv[a + 2];
-                }
-                *(float2 *)(xbuf + (size_t)d*TY*NX + L.xr*NX + x0) = make_float2(o0, o1);
-            };
-            task(std::integral_constant<int, 0>{}); task(std::integral_constant<int, 1>{});
-            task(std::integral_constant<int, 2>{}); task(std::integral_constant<int, 3>{});
-            task(std::integral_constant<int, 4>{});
-        }
-        __syncthreads();
-        {
-            const int o = L.yl*NX + L.xl, st = TY*NX;
-            tmem_st8(tl + ring_col(sp) + 8, xbuf[0*st + o], xbuf[2*st + o], xbuf[1*st + o], xbuf[3*st + o],
-                     xbuf[6*st + o], xbuf[8*st + o], xbuf[7*st + o], xbuf[9*st + o]);
-            tmem_st2(tl + r12_col(p), xbuf[4*st + o], xbuf[5*st + o]);
+            for (int a = 0; a < 7; a++) {
+                const int xx = (L.xl - 3 + a) & (NX - 1);
+                const P2 w = p2(tc.wx0[a], tc.wx2[a]);
+                const float4 g = ybuf[xx];
+                fma2(a78, w, p2(g.x, g.y));
+                fma2(a910, w, p2(g.z, g.w));
+                fma2(a12, w, p2(ldv<S>(raw_row + LY::off(1) + xx), ldv<S>(raw_row + LY::off(2) + xx)));
+                fma2(a1112, w, p2(ldv<S>(raw_row + LY::off(11) + xx), ldv<S>(raw_row + LY::off(12) + xx)));
+                fma2(a1314, w, p2(ldv<S>(raw_row + LY::off(13) + xx), ldv<S>(raw_row + LY::off(14) + xx)));
+            }
+            const float2 v78 = unp(a78), v910 = unp(a910), v12 = unp(a12), v1112 = unp(a1112), v1314 = unp(a1314);
+            tmem_st8(tl + ring_col(sp) + 8, v78.x, v910.x, v78.y, v910.y, v1112.x, v1314.x, v1112.y, v1314.y);
+            tmem_st2(tl + r12_col(p), v12.x, v12.y);
         }
     }
 
@@ -423,10 +406,6 @@ struct TiledKernel {
         L.tid = threadIdx.x;
         L.xl = L.tid & (NX - 1);
         L.yl = L.tid >> LY::LOG2NX;
-        L.xsel = L.tid/(NTHREADS/2);                   // half the threads per departure side
-        const int pair = L.tid & (NTHREADS/2 - 1);     // TY*NX/2 node pairs per plane
-        L.xr = pair >> (LY::LOG2NX - 1);
-        L.xx0 = 2*(pair & (NX/2 - 1));
         return L;
     }
 
