@@ -81,8 +81,21 @@ def main():
     w("                                          T s_nu, T s_pi, T s_m) {\n")
     for p, (a, b) in enumerate(PAIRS):
         w(f"    const T S{p} = d[{a}] + d[{b}], A{p} = d[{a}] - d[{b}];\n")
+    relax_body(w, M, norms, "d[0]")
+    # the same operator from the pair sums / differences of d, given by the caller
+    w("// The same relaxation from d0 = d[0] and the pair sums S[p] = d[a] + d[b] and differences\n")
+    w("// A[p] = d[a] - d[b] of the opposite pairs (a, b) = " + " ".join(f"({a},{b})" for a, b in PAIRS) + ".\n")
+    w("template <typename T>\n__device__ __forceinline__ void mrt_relax_pairs(T (&F)[19], T d0, const T (&S)[9], const T (&A)[9],\n")
+    w("                                                T s_e, T s_eps, T s_q, T s_nu, T s_pi, T s_m) {\n")
+    for p in range(9):
+        w(f"    const T S{p} = S[{p}], A{p} = A[{p}];\n")
+    relax_body(w, M, norms, "d0")
+    tail(w)
+
+
+def relax_body(w, M, norms, d0):
     for c in EVEN:
-        terms = [(M[c][0], "d[0]")] + [(M[c][a], f"S{p}") for p, (a, b) in enumerate(PAIRS)]
+        terms = [(M[c][0], d0)] + [(M[c][a], f"S{p}") for p, (a, b) in enumerate(PAIRS)]
         w(f"    const T r{c} = {RATE[c]}*T(1.0/{norms[c]}.0)*({grouped(terms)});\n")
     for c in ODD:
         terms = [(M[c][a], f"A{p}") for p, (a, b) in enumerate(PAIRS)]
@@ -94,6 +107,9 @@ def main():
         w(f"    {{ const T ev = {ev}, od = {od};\n")
         w(f"      F[{a}] -= ev + od; F[{b}] -= ev - od; }}\n")
     w("}\n\n")
+
+
+def tail(w):
     # second-moment tensor of d (for the Smagorinsky closure): even parity -> pair sums
     w("// Non-equilibrium momentum flux Pi_ab = sum_q e_qa e_qb d_q, returned as Q = Pi:Pi.\n")
     w("template <typename T>\n__device__ __forceinline__ T pi_neq_norm2(const T (&d)[19]) {\n")
@@ -102,6 +118,12 @@ def main():
     comps = {"xx": (0, 0), "yy": (1, 1), "zz": (2, 2), "xy": (0, 1), "yz": (1, 2), "xz": (0, 2)}
     for nm, (i, j) in comps.items():
         terms = [(E[a][i] * E[a][j], f"S{p}") for p, (a, b) in enumerate(PAIRS)]
+        w(f"    const T p{nm} = {grouped(terms)};\n")
+    w("    return pxx*pxx + pyy*pyy + pzz*pzz + T(2)*(pxy*pxy + pyz*pyz + pxz*pxz);\n}\n")
+    w("\n// The same from the pair sums S[p] = d[a] + d[b].\n")
+    w("template <typename T>\n__device__ __forceinline__ T pi_neq_norm2_pairs(const T (&S)[9]) {\n")
+    for nm, (i, j) in comps.items():
+        terms = [(E[a][i] * E[a][j], f"S[{p}]") for p, (a, b) in enumerate(PAIRS)]
         w(f"    const T p{nm} = {grouped(terms)};\n")
     w("    return pxx*pxx + pyy*pyy + pzz*pzz + T(2)*(pxy*pxy + pyz*pyz + pxz*pxz);\n}\n")
 

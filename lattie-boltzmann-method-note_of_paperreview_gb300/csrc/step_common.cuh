@@ -177,6 +177,51 @@ __device__ __forceinline__ void collide_node(C (&F)[19], C rho_modify, C f6, C f
     F[9] -= f12; F[10] -= f12; F[16] -= f12; F[18] -= f12;
 }
 
+// FP32 collision of the tiled kernels: the operator of collide_node computed from the pair
+// sums F[a] + F[b] and differences F[a] - F[b] of the opposite directions (a, b), so that
+// density, momentum, the non-equilibrium pair sums/differences and the relaxation share them
+// (the equilibrium part of a pair is 2 w rho (1 - 1.5 u.u + 4.5 c^2) in the sum and
+// 6 w rho c in the difference, c = e_a . u).
+template <bool LES>
+__device__ __forceinline__ void collide_node_pairs(float (&F)[19], float rho_modify, float f6, float f12, float tau,
+                                                   float lesC, float &rho_s, float &u1, float &v1, float &w1) {
+    constexpr int PA[9] = {1, 3, 5, 7, 8, 11, 12, 15, 16}, PB[9] = {2, 4, 6, 10, 9, 14, 13, 18, 17};
+    F[0] = F[0] + rho_modify;
+    float S[9], A[9];
+#pragma unroll
+    for (int p = 0; p < 9; p++) { S[p] = F[PA[p]] + F[PB[p]]; A[p] = F[PA[p]] - F[PB[p]]; }
+    const float r = ((F[0] + S[0]) + (S[1] + S[2])) + ((S[3] + S[4]) + (S[5] + S[6])) + (S[7] + S[8]);
+    rho_s = r;
+    const float inv = my_rcp<float>(r);
+    u1 = ((A[0] + A[3]) + (A[5] - (A[4] + A[6])))*inv;
+    v1 = ((A[1] + A[3]) + (A[4] + (A[7] - A[8])))*inv;
+    w1 = ((A[2] + A[5]) + (A[6] + (A[7] + A[8])))*inv;
+    const float udot = u1*u1 + v1*v1 + w1*w1;
+    const float base = 1.f - 1.5f*udot;
+    const float a1 = (1.f/18.f)*r, a2 = (1.f/36.f)*r;
+    const float d0 = F[0] - (1.f/3.f)*r*base;
+    {
+        const float cu[9] = {u1, v1, w1, u1 + v1, -u1 + v1, u1 + w1, -u1 + w1, v1 + w1, -v1 + w1};
+#pragma unroll
+        for (int p = 0; p < 9; p++) {
+            const float a = p < 3 ? a1 : a2;
+            S[p] = S[p] - 2.f*a*(base + 4.5f*cu[p]*cu[p]);
+            A[p] = A[p] - 6.f*a*cu[p];
+        }
+    }
+    float s_nu = my_rcp<float>(tau);
+    if constexpr (LES) {
+        const float Qn = pi_neq_norm2_pairs(S);
+        const float nu0 = (tau - 0.5f)*(1.f/3.f);
+        const float Sm = my_div<float>(my_sqrt<float>(nu0*nu0 + 18.f*lesC*my_sqrt<float>(Qn)) - nu0, 6.f*lesC);
+        s_nu = my_rcp<float>(tau + 3.f*lesC*Sm);
+    }
+    mrt_relax_pairs<float>(F, d0, S, A, 1.19f, 1.4f, 1.2f, s_nu, 1.4f, 1.5f);
+    F[3] += f6; F[4] -= f6;
+    F[7] += f12; F[8] += f12; F[15] += f12; F[17] += f12;
+    F[9] -= f12; F[10] -= f12; F[16] -= f12; F[18] -= f12;
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

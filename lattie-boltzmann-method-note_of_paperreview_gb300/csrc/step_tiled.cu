@@ -202,7 +202,7 @@ struct TiledKernel {
 #pragma unroll
         for (int q = 0; q < 19; q++) Fl[q] = F[q];
         float rho_s, u1, v1, w1;
-        collide_node<float, LES>(Fl, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
+        collide_node_pairs<LES>(Fl, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
 #pragma unroll
         for (int q = 0; q < 19; q++) store_f<S>(fn + (size_t)q*N, node, q, Fl[q]);
         if (macros_on) { rho_out[node] = rho_s; u_out[node] = u1; v_out[node] = v1; w_out[node] = w1; }
