@@ -34,7 +34,12 @@ namespace islbm {
 
 namespace {
 
-constexpr int NTHREADS = 128;
+// Threads per CTA for a spanwise width NXC: one node per thread, at least 128 (tiles of
+// 128/NXC full rows), a single row for the widths above 128.
+template <int NXC> constexpr int threads_for() { return NXC < 128 ? 128 : NXC; }
+// TMEM columns of a CTA's xi ring: 128 per 128 threads (each thread's lane holds 126 values),
+// rounded up to a power of two as the allocator requires
+template <int NT> constexpr int ring_cols_for() { return NT <= 128 ? 128 : (NT <= 256 ? 256 : 512); }
 // Copy stages per tile: the next plane is in flight while one is filtered (a third stage for
 // the 2-byte formats, which would fit, measured no faster on GB300).
 template <class S> constexpr int stages_for() { return 2; }
@@ -52,8 +57,10 @@ template <class S> constexpr int stages_for() { return 2; }
 template <class S, int NXC>
 struct Lay {
     static constexpr int NX = NXC;
-    static constexpr int TY = NTHREADS/NXC;
-    static constexpr int LOG2NX = NXC == 8 ? 3 : NXC == 16 ? 4 : NXC == 32 ? 5 : NXC == 64 ? 6 : NXC == 128 ? 7 : 8;
+    static constexpr int NT = threads_for<NXC>();
+    static constexpr int TY = NT/NXC;
+    static constexpr int RING = ring_cols_for<NT>();
+    static constexpr int CTAS_PER_SM = 512/RING;   // TMEM bound (512 columns per SM)
     static constexpr int EB = (int)sizeof(S);
     static constexpr int NS = stages_for<S>();
     static constexpr bool wide(int q) { return q == 3 || q == 4 || (q >= 7 && q <= 10) || q >= 15; }
@@ -92,8 +99,10 @@ struct Lay {
     static constexpr int ybuf_off = NF*front_bytes + NS*stage_bytes;
     static constexpr int bar_off = ybuf_off + 2*TY*NX*16;
     static constexpr int flag_off = bar_off + NS*8;   // CTA-wide "a wait timed out" flag, then the TMEM address
-    // at least 46 KB, so that no more than four CTAs (4 x RING_COLS TMEM columns) share an SM
-    static constexpr int smem_bytes = flag_off + 16 > 46*1024 ? flag_off + 16 : 46*1024;
+    // large enough that no more than CTAS_PER_SM CTAs fit in an SM's 228 KB (1 KB reserved per
+    // CTA), so the TMEM allocations of resident CTAs never exceed the SM's 512 columns
+    static constexpr int smem_floor = 228*1024/(CTAS_PER_SM + 1) + 1;
+    static constexpr int smem_bytes = flag_off + 16 > smem_floor ? flag_off + 16 : smem_floor;
 };
 
 // xi ring in tensor memory: each thread keeps the filtered values of the 7 planes of its
@@ -102,7 +111,6 @@ struct Lay {
 //   columns 112 + 2*(p mod 8), +1: the spanwise-filtered F1, F2 of plane p (used by target p,
 //   which completes at most three planes later).
 // The pairs are chosen so that each pair's xi weights are adjacent in the weight row.
-constexpr int RING_COLS = 128;   // TMEM columns per CTA (power of two >= 32)
 __device__ __forceinline__ int ring_col(int slot) { return 16*slot; }   // slot = p mod 7, tracked by the caller
 __device__ __forceinline__ int r12_col(int p) { return 112 + 2*(p & 7); }
 
@@ -149,6 +157,12 @@ __device__ __forceinline__ void xi_combine(uint32_t tl, int sb, const float *wv_
     t = unp(a810); F[8] = t.x; F[10] = t.y;
     t = unp(a1113); F[11] = t.x; F[13] = t.y;
     t = unp(a1214); F[12] = t.x; F[14] = t.y;
+}
+
+// periodic spanwise index for v in [-NX, 2*NX)
+template <int NX> __device__ __forceinline__ int wrap_x(int v) {
+    if constexpr ((NX & (NX - 1)) == 0) return v & (NX - 1);
+    else return v < 0 ? v + NX : (v >= NX ? v - NX : v);
 }
 
 template <class S, bool LES, int NXC>
@@ -310,7 +324,7 @@ struct TiledKernel {
     // wait anywhere in the CTA (the shared flag, written before the barrier) no copy starts.
     __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, const Piece &P, const Lane &L,
                                           unsigned &parity) const {
-        if ((L.tid & 31) >= 6) return;
+        if ((L.tid & 31) >= 6 || L.tid >= 128) return;   // lanes 0..5 of warps 0..3
         if (*(volatile int *)(smem + LY::flag_off)) return;
         if (p == k.drill_plane) return;   // failure drill: this plane's copies never start
         fence_proxy_async();
@@ -361,7 +375,7 @@ struct TiledKernel {
             P2 a78 = p2(0.f, 0.f), a910 = a78, a12 = a78, a1112 = a78, a1314 = a78;
 #pragma unroll
             for (int a = 0; a < 7; a++) {
-                const int xx = (L.xl - 3 + a) & (NX - 1);
+                const int xx = wrap_x<NX>(L.xl - 3 + a);
                 const P2 w = p2(tc.wx0[a], tc.wx2[a]);
                 const float4 g = ybuf[xx];
                 fma2(a78, w, p2(g.x, g.y));
@@ -404,8 +418,8 @@ struct TiledKernel {
         constexpr int NX = LY::NX;
         Lane L;
         L.tid = threadIdx.x;
-        L.xl = L.tid & (NX - 1);
-        L.yl = L.tid >> LY::LOG2NX;
+        L.xl = L.tid % NX;
+        L.yl = L.tid / NX;
         return L;
     }
 
@@ -442,17 +456,18 @@ struct TiledKernel {
         }
     }
 
-    // TMEM ring: warp 0 allocates RING_COLS columns, every thread reads the base address
+    // TMEM ring: warp 0 allocates LY::RING columns; every thread gets the address of its lane
+    // (lane quarter w % 4 of warp w) and of its 128-column block (w / 4)
     __device__ __forceinline__ uint32_t ring_alloc(unsigned char *smem, int tid) const {
         uint32_t *slot = (uint32_t *)(smem + LY::flag_off + 8);
         if (tid < 32) {
-            tmem_alloc(slot, RING_COLS);
+            tmem_alloc(slot, LY::RING);
             tmem_relinquish();
         }
         tmem_fence_before();
         __syncthreads();
         tmem_fence_after();
-        return *(volatile uint32_t *)slot + ((uint32_t)(32*((tid >> 5) & 3)) << 16);
+        return *(volatile uint32_t *)slot + ((uint32_t)(32*((tid >> 5) & 3)) << 16) + (uint32_t)(128*(tid >> 7));
     }
     __device__ __forceinline__ void ring_free(unsigned char *smem, int tid) const {
         tmem_wait_ld();
@@ -461,7 +476,7 @@ struct TiledKernel {
         __syncthreads();
         if (tid < 32) {
             tmem_fence_after();
-            tmem_dealloc(*(volatile uint32_t *)(smem + LY::flag_off + 8), RING_COLS);
+            tmem_dealloc(*(volatile uint32_t *)(smem + LY::flag_off + 8), LY::RING);
         }
     }
 
@@ -501,7 +516,7 @@ struct TiledKernel {
         }
         drain(smem, parity, L.tid);
         ring_free(smem, L.tid);
-        end_of_step<NTHREADS>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0,
+        end_of_step<LY::NT>(ctrl, k, tc.n, ub_total, mass_total, true, mass_on != 0,
                               gridDim.x*gridDim.y*gridDim.z);
     }
 };
@@ -519,10 +534,11 @@ struct BatchDesc {
 };
 
 template <class S, bool LES, int NXC>
-__global__ void __launch_bounds__(NTHREADS, 4) step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
+__global__ void __launch_bounds__(threads_for<NXC>(), 512/threads_for<NXC>())
+step_tiled_kernel(TiledKernel<S, LES, NXC> K) { K.run(); }
 
 template <class S, bool LES, int NXC>
-__global__ void __launch_bounds__(NTHREADS, 4)
+__global__ void __launch_bounds__(threads_for<NXC>(), 512/threads_for<NXC>())
 step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const int2 *__restrict__ items, int nitems,
                         int macros_on) {
     using KT = TiledKernel<S, LES, NXC>;
@@ -547,7 +563,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         {
             const unsigned *src = (const unsigned *)&descs[w.x].K;
             unsigned *dst = (unsigned *)kbuf;
-            for (int i = tid; i < (int)(sizeof(KT)/4); i += NTHREADS) dst[i] = src[i];
+            for (int i = tid; i < (int)(sizeof(KT)/4); i += LY::NT) dst[i] = src[i];
         }
         if (tid == 0) step_s = *(volatile unsigned long long *)&descs[w.x].K.ctrl->step;
         __syncthreads();
@@ -566,7 +582,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         P.y0 = w.y*LY::TY; P.ta = 0; P.tb = K.k.NZ; P.p0 = 0; P.p1 = K.k.NZ - 1;
         float ub = 0.f, mass = 0.f;
         K.piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
-        end_of_step<NTHREADS>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
+        end_of_step<LY::NT>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
                               (unsigned)descs[w.x].ntiles);
     }
     __syncthreads();
@@ -594,7 +610,7 @@ cudaError_t launch_t(const StepLaunch &L) {
         if (e != cudaSuccess) return e;
         attr_done = true;
     }
-    step_tiled_kernel<S, LES, NXC><<<K.tc.grid, NTHREADS, smem, L.stream>>>(K);
+    step_tiled_kernel<S, LES, NXC><<<K.tc.grid, Lay<S, NXC>::NT, smem, L.stream>>>(K);
     return cudaGetLastError();
 }
 
@@ -603,7 +619,10 @@ cudaError_t launch_nx(const StepLaunch &L) {
     switch (L.k.NX) {
     case 32: return launch_t<S, LES, 32>(L);
     case 64: return launch_t<S, LES, 64>(L);
-    default: return launch_t<S, LES, 128>(L);
+    case 128: return launch_t<S, LES, 128>(L);
+    case 256: return launch_t<S, LES, 256>(L);
+    case 384: return launch_t<S, LES, 384>(L);
+    default: return cudaErrorNotSupported;
     }
 }
 
@@ -612,18 +631,31 @@ cudaError_t launch_s(const StepLaunch &L) {
     return L.les ? launch_nx<S, true>(L) : launch_nx<S, false>(L);
 }
 
+template <class S> struct LayInfo {
+    size_t smem;
+    int nt, ctas_per_sm;
+};
+template <class S, int NXC> LayInfo<S> lay_info() {
+    return {(size_t)Lay<S, NXC>::smem_bytes, Lay<S, NXC>::NT, Lay<S, NXC>::CTAS_PER_SM};
+}
 template <class S>
-size_t smem_for(int nx) {
-    return nx == 32 ? Lay<S, 32>::smem_bytes : (nx == 64 ? Lay<S, 64>::smem_bytes : Lay<S, 128>::smem_bytes);
+LayInfo<S> lay_for(int nx) {
+    switch (nx) {
+    case 32: return lay_info<S, 32>();
+    case 64: return lay_info<S, 64>();
+    case 128: return lay_info<S, 128>();
+    case 256: return lay_info<S, 256>();
+    default: return lay_info<S, 384>();
+    }
 }
 
 }  // namespace
 
 bool tiled_supported(const StepConst &k, int precision) {
     if (precision == ISLBM_FP64) return false;
-    // spanwise widths with a compiled layout (a tile is 256 nodes)
-    if (k.NX != 32 && k.NX != 64 && k.NX != 128) return false;
-    const int TY = NTHREADS/k.NX;
+    // spanwise widths with a compiled layout (tiles of 128 nodes; one row of 256 or 384)
+    if (k.NX != 32 && k.NX != 64 && k.NX != 128 && k.NX != 256 && k.NX != 384) return false;
+    const int TY = k.NX < 128 ? 128/k.NX : 1;
     if (k.NY % TY != 0 || k.NY < TY + 6 || k.NZ < 8) return false;
     return true;
 }
@@ -632,11 +664,15 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
                      const double *wy2, int num_sms, TiledConst *out) {
     TiledConst tc;
     std::memset(&tc, 0, sizeof(tc));
-    tc.TY = NTHREADS/k.NX;
+    tc.TY = k.NX < 128 ? 128/k.NX : 1;
     int l = 0;
     while ((1 << l) < k.NX) l++;
     tc.log2nx = l;
-    tc.smem_bytes = precision == ISLBM_FP32 ? smem_for<float>(k.NX) : smem_for<__half>(k.NX);
+    size_t smem;
+    int ctas_tmem;
+    if (precision == ISLBM_FP32) { const auto li = lay_for<float>(k.NX); smem = li.smem; ctas_tmem = li.ctas_per_sm; }
+    else { const auto li = lay_for<__half>(k.NX); smem = li.smem; ctas_tmem = li.ctas_per_sm; }
+    tc.smem_bytes = smem;
     for (int a = 0; a < 7; a++) {
         tc.wx0[a] = (float)wx0[a]; tc.wx2[a] = (float)wx2[a];
         tc.wy0[a] = (float)wy0[a]; tc.wy2[a] = (float)wy2[a];
@@ -644,8 +680,8 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     const int tiles = k.NY/tc.TY;
     tc.units = (long long)tiles*k.NZ;
     // persistent CTAs: as many as fit on the SMs by shared memory (228 KB per SM, 1 KB reserved
-    // per CTA), at most four (the register bound of the kernel and the TMEM ring's share)
-    const int per_sm = (int)std::min<size_t>(4, (228*1024)/(tc.smem_bytes + 1024));
+    // per CTA) and by the TMEM rings (512 columns per SM; also the register bound of the kernel)
+    const int per_sm = (int)std::min<size_t>((size_t)ctas_tmem, (228*1024)/(tc.smem_bytes + 1024));
     const int slots = per_sm*num_sms;
     // wall-normal segments per column: enough items to fill the resident slots, each at
     // least 16 targets long (a segment re-reads the 6 planes below it to fill its ring)
@@ -697,7 +733,7 @@ struct BatchOps {
     static cudaError_t launch(const void *descs, const int2 *items, int nitems, int grid, int macros_on, cudaStream_t st) {
         cudaError_t e = prepare();
         if (e != cudaSuccess) return e;
-        step_tiled_batch_kernel<S, LES, NXC><<<grid, NTHREADS, Lay<S, NXC>::smem_bytes, st>>>((const D *)descs, items,
+        step_tiled_batch_kernel<S, LES, NXC><<<grid, Lay<S, NXC>::NT, Lay<S, NXC>::smem_bytes, st>>>((const D *)descs, items,
                                                                                              nitems, macros_on);
         return cudaGetLastError();
     }
@@ -711,7 +747,9 @@ auto dispatch(int precision, int NX, bool les, F &&f) {
         switch (NX) {
         case 32: return f(BatchOps<S, L, 32>{});
         case 64: return f(BatchOps<S, L, 64>{});
-        default: return f(BatchOps<S, L, 128>{});
+        case 128: return f(BatchOps<S, L, 128>{});
+        case 256: return f(BatchOps<S, L, 256>{});
+        default: return f(BatchOps<S, L, 384>{});
         }
     };
     auto by_les = [&](auto s_tag) {
