@@ -131,6 +131,31 @@ def device_run(islbm, torch, precision, steps, warmup, device):
     return {"ms": ms, "mlups": n * steps / (ms * 1e-3) / 1e6, "healthy": ok, "fields": fields}
 
 
+LARGE = dict(NX=384, NY=768, NZ=512, Re=10595.0, Uref=0.04, NDTFRC=100, les_cs=0.1)
+
+
+def large_run(islbm, torch, device, steps=10, warmup=3):
+    """The large single solve (768x384x512, 151M nodes, Re_h 10595, LES): FP32 and FP16-deviation
+    storage on the tiled kernel, MLUPS and HBM fraction, and the xi weight-table bytes stored per
+    (y, z) against per node."""
+    n = LARGE["NX"] * LARGE["NY"] * LARGE["NZ"]
+    peak, _ = measured_peak_gbs()
+    out = {"grid": "NY768 NX384 NZ512", "nodes": n, "steps": steps}
+    for prec, eb in (("fp32", 4), ("fp16", 2)):
+        p = islbm.default_params(precision=prec, device=device, **LARGE)
+        with islbm.Solver(p) as s:
+            s.step(warmup)
+            s.sync()
+            ms = time_steps(islbm, torch, s, steps)
+            if prec == "fp32":
+                wt = s.weight_table_bytes()
+                out["weight_table_bytes"] = {"per_y_z": wt["stored"], "per_node": wt["per_node"]}
+        mlups = n * steps / (ms * 1e-3) / 1e6
+        gbs = 2 * 19 * eb * n / (ms * 1e-3 / steps) / 1e9
+        out[prec] = {"mlups": mlups, "hbm_gbs": gbs, "frac": gbs / peak, "ms_per_step": ms / steps}
+    return out
+
+
 def e2e_run(islbm, precision, steps, device, f_host):
     """Through the C ABI with host buffers: upload state, step, read fields every 100 steps."""
     import numpy as np
@@ -257,6 +282,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=16)
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -340,6 +366,8 @@ def main():
         line["cpu_baseline"] = {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
                                 "sample": f"{args.cpu_steps} steps of the full 256x128x192 grid, FP64, LES",
                                 "seconds": dt}
+    if rank == 0 and not args.no_large:
+        line["large"] = large_run(islbm, torch, local)
     if rank == 0 and not args.no_serve:
         line["serve"] = serve_run(islbm, args.serve_requests, local)
     if rank == 0:

@@ -222,8 +222,7 @@ struct TiledKernel {
         if (macros_on) { rho_out[node] = rho_s; u_out[node] = u1; v_out[node] = v1; w_out[node] = w1; }
         // column partials in FP32 (at most NZ terms), folded into FP64 once per column
         if (y == k.yplane) ub += v1*T.dxf[x]*T.dzf[z];
-        mass += rho_s;
-        if (!(rho_s == rho_s)) ctrl->nonfinite = 1u;
+        mass += rho_s;   // a non-finite density makes the thread's mass sum non-finite (checked once per piece)
     }
 
     // Copy jobs of a plane (1..18: population q, two pieces when the halo wraps; 19, 20: the
@@ -511,6 +510,7 @@ struct TiledKernel {
             P.p1 = window_base(P.tb - 1) + 6;
             float ub = 0.f, mass = 0.f;   // this piece's partial sums
             piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
+            if (!isfinite(mass)) ctrl->nonfinite = 1u;
             ub_total += (double)ub;
             mass_total += (double)mass;
         }
@@ -582,6 +582,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         P.y0 = w.y*LY::TY; P.ta = 0; P.tb = K.k.NZ; P.p0 = 0; P.p1 = K.k.NZ - 1;
         float ub = 0.f, mass = 0.f;
         K.piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
+        if (!isfinite(mass)) K.ctrl->nonfinite = 1u;
         end_of_step<LY::NT>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
                               (unsigned)descs[w.x].ntiles);
     }
