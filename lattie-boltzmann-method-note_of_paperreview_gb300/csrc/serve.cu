@@ -261,21 +261,32 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
         const size_t db = batch_desc_bytes(g->precision, g->NX, g->les);
         std::vector<unsigned char> hd(db*g->members.size());
         std::vector<int2> items;
-        int maxt = 0;
+        int maxt = 0, total_tiles = 0, min_nz = 1 << 30;
         for (size_t m = 0; m < g->members.size(); m++) {
             islbm_handle *h = g->members[m]->h;
             const int ntiles = h->p.NY/h->tiled.TY;
             maxt = std::max(maxt, ntiles);
+            total_tiles += ntiles;
+            min_nz = std::min(min_nz, h->p.NZ);
+        }
+        // wall-normal segments per column: enough work items for four CTAs per SM, each segment
+        // at least 16 targets long (a segment re-reads the 6 planes below it to fill its ring)
+        const int nseg = std::max(1, std::min(4*s->sms/std::max(1, total_tiles), min_nz/16));
+        for (size_t m = 0; m < g->members.size(); m++) {
+            islbm_handle *h = g->members[m]->h;
             g->nodes += (long long)h->N;
             fill_batch_desc(g->precision, g->NX, g->les, h->tf, h->k, h->tiled, h->ctrl, h->macros, h->fbuf[0], h->fbuf[1],
-                            ntiles, hd.data() + m*db);
+                            h->p.NY/h->tiled.TY, nseg, hd.data() + m*db);
         }
-        // interleave the solves' tiles so that neighbouring tiles of a solve run together
-        for (int t = 0; t < maxt; t++)
-            for (size_t m = 0; m < g->members.size(); m++) {
-                islbm_handle *h = g->members[m]->h;
-                if (t < h->p.NY/h->tiled.TY) items.push_back(make_int2((int)m, t));
-            }
+        // segment-major, the solves' tiles interleaved, so that neighbouring tiles of a solve at
+        // the same height run together
+        for (int seg = 0; seg < nseg; seg++)
+            for (int t = 0; t < maxt; t++)
+                for (size_t m = 0; m < g->members.size(); m++) {
+                    islbm_handle *h = g->members[m]->h;
+                    const int nt = h->p.NY/h->tiled.TY;
+                    if (t < nt) items.push_back(make_int2((int)m, seg*nt + t));
+                }
         g->nitems = (int)items.size();
         SK(cudaMalloc(&g->descs, hd.size()));
         SK(cudaMalloc(&g->items, items.size()*sizeof(int2)));

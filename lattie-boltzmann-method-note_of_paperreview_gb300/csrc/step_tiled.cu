@@ -530,7 +530,8 @@ template <class S, bool LES, int NXC>
 struct BatchDesc {
     TiledKernel<S, LES, NXC> K;
     S *buf[2];          // population buffers; the old one is buf[step & 1]
-    int ntiles;         // work items of this solve per step
+    int ntiles;         // tiles of this solve
+    int nseg;           // wall-normal segments per column (work items per step: ntiles*nseg)
 };
 
 template <class S, bool LES, int NXC>
@@ -578,13 +579,19 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
         __syncthreads();
         const auto L = K.lane();
         const auto sc = K.scalars();
+        const int nt = descs[w.x].ntiles, ns = descs[w.x].nseg;
+        const int tile = w.y % nt, seg = w.y/nt;
         typename KT::Piece P;
-        P.y0 = w.y*LY::TY; P.ta = 0; P.tb = K.k.NZ; P.p0 = 0; P.p1 = K.k.NZ - 1;
+        P.y0 = tile*LY::TY;
+        P.ta = seg*K.k.NZ/ns;
+        P.tb = (seg + 1)*K.k.NZ/ns;
+        P.p0 = K.window_base(P.ta);
+        P.p1 = K.window_base(P.tb - 1) + 6;
         float ub = 0.f, mass = 0.f;
         K.piece(P, smem, parity, faulted, L, tl, sc, ub, mass);
         if (!isfinite(mass)) K.ctrl->nonfinite = 1u;
         end_of_step<LY::NT>(K.ctrl, K.k, K.tc.n, (double)ub, (double)mass, true, K.mass_on != 0,
-                              (unsigned)descs[w.x].ntiles);
+                              (unsigned)(nt*ns));
     }
     __syncthreads();
     if (nitems > 0) K.drain(smem, parity, tid);
@@ -710,7 +717,7 @@ struct BatchOps {
     using D = BatchDesc<S, LES, NXC>;
     static size_t bytes() { return sizeof(D); }
     static void fill(const Tables<float> &T, const StepConst &k, const TiledConst &tc, Ctrl *ctrl, void *const macros[4],
-                     void *buf0, void *buf1, int ntiles, void *out) {
+                     void *buf0, void *buf1, int ntiles, int nseg, void *out) {
         D d;
         std::memset((void *)&d, 0, sizeof(d));
         d.K.T = T; d.K.k = k; d.K.tc = tc; d.K.ctrl = ctrl;
@@ -718,6 +725,7 @@ struct BatchOps {
         d.K.v_out = (float *)macros[2]; d.K.w_out = (float *)macros[3];
         d.buf[0] = (S *)buf0; d.buf[1] = (S *)buf1;
         d.ntiles = ntiles;
+        d.nseg = nseg;
         std::memcpy(out, (const void *)&d, sizeof(d));
     }
     static cudaError_t prepare() {
@@ -770,9 +778,9 @@ size_t batch_desc_bytes(int precision, int NX, bool les) {
 }
 
 void fill_batch_desc(int precision, int NX, bool les, const Tables<float> &T, const StepConst &k, const TiledConst &tc,
-                     Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, void *out) {
+                     Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, int nseg, void *out) {
     dispatch(precision, NX, les, [&](auto ops) {
-        decltype(ops)::fill(T, k, tc, ctrl, macros, buf0, buf1, ntiles, out);
+        decltype(ops)::fill(T, k, tc, ctrl, macros, buf0, buf1, ntiles, nseg, out);
         return 0;
     });
 }

@@ -23,10 +23,11 @@ struct TiledConst {
 int make_tiled_const(const StepConst &k, int precision, const double *wx0, const double *wx2, const double *wy0,
                      const double *wy2, int num_sms, TiledConst *out);
 
-// Batched tiled step: one launch advances every solve described in `descs` by one step.
+// Batched tiled step: one launch advances every solve described in `descs` by one step. Work
+// items are (solve, seg*ntiles + tile): wall-normal segment seg of tile `tile`.
 size_t batch_desc_bytes(int precision, int NX, bool les);
 void fill_batch_desc(int precision, int NX, bool les, const Tables<float> &T, const StepConst &k, const TiledConst &tc,
-                     Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, void *out);
+                     Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, int nseg, void *out);
 // one-time kernel attributes; call before the first launch is captured into a graph
 cudaError_t prepare_step_tiled_batch(int precision, int NX, bool les);
 cudaError_t launch_step_tiled_batch(int precision, int NX, bool les, const void *descs, const int2 *items, int nitems,
