@@ -353,7 +353,7 @@ struct TiledKernel {
             P2 a34 = p2(0.f, 0.f), a1516 = a34, a1718 = a34, a79 = a34, a810 = a34;
 #pragma unroll
             for (int b = 0; b < 7; b++) {
-                const P2 w = p2(tc.wy0[b], tc.wy2[b]);
+                const P2 w = p2(tc.wy[b]);
                 fma2(a34, w, p2(ldv<S>(row(3, b)), ldv<S>(row(4, b))));
                 fma2(a1516, w, p2(ldv<S>(row(15, b)), ldv<S>(row(16, b))));
                 fma2(a1718, w, p2(ldv<S>(row(17, b)), ldv<S>(row(18, b))));
@@ -375,7 +375,7 @@ struct TiledKernel {
 #pragma unroll
             for (int a = 0; a < 7; a++) {
                 const int xx = wrap_x<NX>(L.xl - 3 + a);
-                const P2 w = p2(tc.wx0[a], tc.wx2[a]);
+                const P2 w = p2(tc.wx[a]);
                 const float4 g = ybuf[xx];
                 fma2(a78, w, p2(g.x, g.y));
                 fma2(a910, w, p2(g.z, g.w));
@@ -682,8 +682,8 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     else { const auto li = lay_for<__half>(k.NX); smem = li.smem; ctas_tmem = li.ctas_per_sm; }
     tc.smem_bytes = smem;
     for (int a = 0; a < 7; a++) {
-        tc.wx0[a] = (float)wx0[a]; tc.wx2[a] = (float)wx2[a];
-        tc.wy0[a] = (float)wy0[a]; tc.wy2[a] = (float)wy2[a];
+        tc.wx[a] = make_float2((float)wx0[a], (float)wx2[a]);
+        tc.wy[a] = make_float2((float)wy0[a], (float)wy2[a]);
     }
     const int tiles = k.NY/tc.TY;
     tc.units = (long long)tiles*k.NZ;

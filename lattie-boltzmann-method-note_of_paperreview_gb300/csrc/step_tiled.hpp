@@ -16,7 +16,9 @@ struct TiledConst {
     long long units;              // tiles * NZ (flattened work)
     int log2nx;
     size_t smem_bytes;            // dynamic shared memory per CTA (layout: Lay in step_tiled.cu)
-    float wx0[7], wx2[7], wy0[7], wy2[7];   // uniform-spacing Lagrange weights
+    // uniform-spacing Lagrange weights as (departure - minSize, departure + minSize) pairs, the
+    // operand layout of the packed FP32x2 filters: wx[a] = (wx0[a], wx2[a]), wy[b] = (wy0[b], wy2[b])
+    float2 wx[7], wy[7];
     unsigned long long n;         // step number (set per launch)
 };
 
