@@ -229,18 +229,28 @@ struct TiledKernel {
     // target's xi weights and f0 row). Jobs are spread over the four warps (job q on warp q & 3,
     // lane q >> 2) so that no warp serialises all the copy issues; thread 0 posts the expected
     // bytes (a copy may complete before that: the phase cannot end while the arrival is due).
-    // Copy job Q (compile-time) of plane p into stage s.
-    template <int Q>
-    __device__ __forceinline__ void copy_job(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt) const {
+    struct Lane {
+        int tid, xl, yl;        // node of this thread within the tile
+        // copy job of this lane (lanes 0..5 of warps 0..3: job 4*lane + warp; -1: none)
+        int jq, joff;           // population (19, 20: target weights, f0 row), byte offset in its region
+        bool jfront, jwide;     // region: front buffer or stage; rows: TY + 6 or TY
+    };
+
+    // Copy job of one lane (fixed for the whole kernel, see Lane): population jq of plane p
+    // into its region (front buffer or stage s), as TY rows or TY + 6 rows with the streamwise
+    // halo (two pieces when the halo wraps); jobs 19 and 20 are the target's xi weights and f0
+    // row (only when the plane carries a target). Thread 0 posts the expected bytes first (a
+    // copy may complete before that: the phase cannot end while the arrival is due).
+    __device__ void issue_plane(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt, const Lane &L) const {
         constexpr int NX = LY::NX, TY = LY::TY;
         const int NY = k.NY;
-        const unsigned row_bytes = (unsigned)(NX*sizeof(S));
+        constexpr unsigned row_bytes = (unsigned)(NX*sizeof(S));
+        if (L.tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
         unsigned char *stage = smem + LY::stage_off(s);
-        if constexpr (Q < 19) {
-            const size_t N = (size_t)NX*NY*k.NZ;
-            S *dst = (S *)(LY::front(Q) ? smem + LY::front_off(s) : stage) + LY::off(Q);
-            const S *plane_base = fo + (size_t)Q*N + (size_t)p*NY*NX;
-            if constexpr (!LY::wide(Q)) {
+        if (L.jq >= 1 && L.jq < 19) {
+            S *dst = (S *)((L.jfront ? smem + LY::front_off(s) : stage) + L.joff);
+            const S *plane_base = fo + (size_t)L.jq*((size_t)NX*NY*k.NZ) + (size_t)p*NY*NX;
+            if (!L.jwide) {
                 bulk_g2s(dst, plane_base + (size_t)y0*NX, TY*row_bytes, bar);
             } else {
                 const int ys = y0 >= 3 ? y0 - 3 : y0 - 3 + NY;
@@ -249,38 +259,9 @@ struct TiledKernel {
                 bulk_g2s(dst, plane_base + (size_t)ys*NX, first*row_bytes, bar);
                 if (first < rows) bulk_g2s(dst + (size_t)first*NX, plane_base, (rows - first)*row_bytes, bar);
             }
-        } else if constexpr (Q == 19) {
-            if (tgt) bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)(p - 3)*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
-        } else {
-            if (tgt) bulk_g2s(stage + LY::f0_off, fo + ((size_t)(p - 3)*NY + y0)*NX, TY*row_bytes, bar);
-        }
-    }
-
-    __device__ void issue_plane(unsigned char *smem, int s, uint64_t *bar, int p, int y0, bool tgt, int tid) const {
-        if (tid == 0) mbar_expect_tx(bar, LY::pops_bytes() + (tgt ? LY::tgt_bytes : 0u));
-        // job q = 4*lane + warp (lanes 0..5), dispatched to compile-time job bodies
-        switch (4*(tid & 31) + (tid >> 5)) {
-        case 1: copy_job<1>(smem, s, bar, p, y0, tgt); break;
-        case 2: copy_job<2>(smem, s, bar, p, y0, tgt); break;
-        case 3: copy_job<3>(smem, s, bar, p, y0, tgt); break;
-        case 4: copy_job<4>(smem, s, bar, p, y0, tgt); break;
-        case 5: copy_job<5>(smem, s, bar, p, y0, tgt); break;
-        case 6: copy_job<6>(smem, s, bar, p, y0, tgt); break;
-        case 7: copy_job<7>(smem, s, bar, p, y0, tgt); break;
-        case 8: copy_job<8>(smem, s, bar, p, y0, tgt); break;
-        case 9: copy_job<9>(smem, s, bar, p, y0, tgt); break;
-        case 10: copy_job<10>(smem, s, bar, p, y0, tgt); break;
-        case 11: copy_job<11>(smem, s, bar, p, y0, tgt); break;
-        case 12: copy_job<12>(smem, s, bar, p, y0, tgt); break;
-        case 13: copy_job<13>(smem, s, bar, p, y0, tgt); break;
-        case 14: copy_job<14>(smem, s, bar, p, y0, tgt); break;
-        case 15: copy_job<15>(smem, s, bar, p, y0, tgt); break;
-        case 16: copy_job<16>(smem, s, bar, p, y0, tgt); break;
-        case 17: copy_job<17>(smem, s, bar, p, y0, tgt); break;
-        case 18: copy_job<18>(smem, s, bar, p, y0, tgt); break;
-        case 19: copy_job<19>(smem, s, bar, p, y0, tgt); break;
-        case 20: copy_job<20>(smem, s, bar, p, y0, tgt); break;
-        default: break;
+        } else if (tgt && L.jq >= 19) {
+            if (L.jq == 19) bulk_g2s(stage + LY::w_off, T.wxi + ((size_t)(p - 3)*NY + y0)*64, (unsigned)(TY*64*sizeof(float)), bar);
+            if (L.jq == 20) bulk_g2s(stage + LY::f0_off, fo + ((size_t)(p - 3)*NY + y0)*NX, TY*row_bytes, bar);
         }
     }
 
@@ -298,10 +279,6 @@ struct TiledKernel {
             }
         }
     }
-
-    struct Lane {
-        int tid, xl, yl;        // node of this thread within the tile
-    };
 
     // A piece of a column: targets ta .. tb-1 of tile rows y0 .. y0+TY-1, computed from source
     // planes p0 .. p1 (target t uses planes b(t) .. b(t)+6, see window_base).
@@ -323,11 +300,11 @@ struct TiledKernel {
     // wait anywhere in the CTA (the shared flag, written before the barrier) no copy starts.
     __device__ __forceinline__ void issue(unsigned char *smem, int s, int p, const Piece &P, const Lane &L,
                                           unsigned &parity) const {
-        if ((L.tid & 31) >= 6 || L.tid >= 128) return;   // lanes 0..5 of warps 0..3
+        if (L.jq < 0) return;   // lanes 0..5 of warps 0..3 (job 0: thread 0, which only posts the bytes)
         if (*(volatile int *)(smem + LY::flag_off)) return;
         if (p == k.drill_plane) return;   // failure drill: this plane's copies never start
         fence_proxy_async();
-        issue_plane(smem, s, (uint64_t *)(smem + LY::bar_off) + s, p, P.y0, staged_target(p, P), L.tid);
+        issue_plane(smem, s, (uint64_t *)(smem + LY::bar_off) + s, p, P.y0, staged_target(p, P), L);
         if (L.tid == 0)
             parity = (parity & ~(1u << (PPAR + s))) | (((parity >> s) & 1u) << (PPAR + s)) | (1u << (PEND + s));
     }
@@ -419,6 +396,12 @@ struct TiledKernel {
         L.tid = threadIdx.x;
         L.xl = L.tid % NX;
         L.yl = L.tid / NX;
+        int q = ((L.tid & 31) < 6 && L.tid < 128) ? 4*(L.tid & 31) + (L.tid >> 5) : -1;
+        if (q > 20) q = -1;   // jobs 0..20 only
+        L.jq = q; L.joff = 0; L.jfront = false; L.jwide = false;
+#pragma unroll
+        for (int r = 1; r < 19; r++)
+            if (q == r) { L.joff = LY::off_bytes(r); L.jfront = LY::front(r); L.jwide = LY::wide(r); }
         return L;
     }
 
