@@ -181,6 +181,9 @@ struct TiledKernel {
 
     // Walls, BFL rows, collision and store of one node whose streamed populations are in F
     // (F[1..18] as filtered values, deviations for the deviation formats; F[0] full).
+    // CAP: a wall-cap target (z <= 3 or z >= NZ-4), the only ones that can be wall rows (bounce-back
+    // at z = 0 and NZ-1, BFL rows at z <= 1).
+    template <bool CAP>
     __device__ __forceinline__ void finish(float *F, int x, int y, int z, const Scal &sc, float &ub, float &mass) const {
         constexpr int NX = LY::NX;
         const int NY = k.NY;
@@ -190,17 +193,17 @@ struct TiledKernel {
 #pragma unroll
             for (int q = 1; q < 19; q++) F[q] += (float)dev_ref(q);
         }
-        if (z == 0) {
+        if (CAP && z == 0) {
             const S *b = fo + node;
             F[5] = load_f<S>(b + 6*N, 0, 6); F[11] = load_f<S>(b + 14*N, 0, 14); F[12] = load_f<S>(b + 13*N, 0, 13);
             F[15] = load_f<S>(b + 18*N, 0, 18); F[16] = load_f<S>(b + 17*N, 0, 17);
         }
-        if (z == k.NZ - 1) {
+        if (CAP && z == k.NZ - 1) {
             const S *b = fo + node;
             F[6] = load_f<S>(b + 5*N, 0, 5); F[13] = load_f<S>(b + 12*N, 0, 12); F[14] = load_f<S>(b + 11*N, 0, 11);
             F[17] = load_f<S>(b + 16*N, 0, 16); F[18] = load_f<S>(b + 15*N, 0, 15);
         }
-        if (z <= 1) {
+        if (CAP && z <= 1) {
             const int nb = 2*k.NYD6, r = z*k.NYD6 + (y + 3);
             if (T.bfl_flag[r] | T.bfl_flag[nb + r] | T.bfl_flag[2*nb + r] | T.bfl_flag[3*nb + r]) {
                 // the out-of-line BFL rows work on a copy, so that F itself never needs an address
@@ -369,25 +372,40 @@ struct TiledKernel {
     // Target t of tile row y, whose window (planes p-6 .. p) is complete in the ring. Staged
     // targets take their xi weights and f0 row from the stage of plane p; the wall caps read them
     // from global memory.
-    __device__ __forceinline__ void target(uint32_t tl, int sp, int t, bool staged, const unsigned char *stage, int x,
-                                           int y, int yl, const Scal &sc, float &ub, float &mass) const {
+    __device__ __forceinline__ void target(uint32_t tl, int sp, int t, const unsigned char *stage, int x, int y, int yl,
+                                           const Scal &sc, float &ub, float &mass) const {
         constexpr int NX = LY::NX;
         float F[19];
         tmem_wait_st();   // this thread's ring stores of plane p are complete
-        // window base p - 6 sits in slot (sp + 1) mod 7; separate calls keep each weight pointer
-        // in its own address space (shared or global)
-        const int sb = sp == 6 ? 0 : sp + 1;
-        if (staged) xi_combine(tl, sb, (const float *)(stage + LY::w_off) + yl*64, F);
-        else xi_combine(tl, sb, T.wxi + ((size_t)t*k.NY + y)*64, F);
+        // window base p - 6 sits in slot (sp + 1) mod 7
+        xi_combine(tl, sp == 6 ? 0 : sp + 1, (const float *)(stage + LY::w_off) + yl*64, F);
         {
             uint32_t r[2];
             tmem_ld2(tl + r12_col(t), r);
             tmem_wait_ld(r);
             F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
         }
-        if (staged) F[0] = ld1<S>((const S *)(stage + LY::f0_off) + yl*NX + x, (float)dev_ref(0));
-        else F[0] = load_f<S>(fo, ((size_t)t*k.NY + y)*NX + x, 0);
-        finish(F, x, y, t, sc, ub, mass);
+        F[0] = ld1<S>((const S *)(stage + LY::f0_off) + yl*NX + x, (float)dev_ref(0));
+        finish<false>(F, x, y, t, sc, ub, mass);
+    }
+
+    // A wall-cap target (z <= 3 at the window of plane 6, z >= NZ-3 at the window of plane NZ-1):
+    // xi weights and f0 from global memory, walls and BFL rows. Out of line, so that the plane
+    // loop's code stays small; returns the target's (ub, mass) contributions.
+    __device__ __noinline__ float2 cap_target(uint32_t tl, int sp, int t, int x, int y, const Scal &sc) const {
+        float F[19];
+        tmem_wait_st();
+        xi_combine(tl, sp == 6 ? 0 : sp + 1, T.wxi + ((size_t)t*k.NY + y)*64, F);
+        {
+            uint32_t r[2];
+            tmem_ld2(tl + r12_col(t), r);
+            tmem_wait_ld(r);
+            F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
+        }
+        F[0] = load_f<S>(fo, ((size_t)t*k.NY + y)*LY::NX + x, 0);
+        float ub = 0.f, mass = 0.f;
+        finish<true>(F, x, y, t, sc, ub, mass);
+        return make_float2(ub, mass);
     }
 
     __device__ __forceinline__ Lane lane() const {
@@ -433,8 +451,15 @@ struct TiledKernel {
             if (i < 6) continue;   // window of plane p not yet in the ring
             const unsigned char *stage = smem + LY::stage_off(i % LY::NS);
             const int lo = p == 6 ? 0 : p - 3, hi = p == NZ - 1 ? NZ - 1 : p - 3;
-            for (int t = max(lo, P.ta); t <= min(hi, P.tb - 1); t++)
-                target(tl, sp, t, t == p - 3 && staged_target(p, P), stage, L.xl, y, L.yl, sc, ub, mass);
+            for (int t = max(lo, P.ta); t <= min(hi, P.tb - 1); t++) {
+                if (t == p - 3 && staged_target(p, P)) {
+                    target(tl, sp, t, stage, L.xl, y, L.yl, sc, ub, mass);
+                } else {
+                    const float2 c = cap_target(tl, sp, t, L.xl, y, sc);
+                    ub += c.x;
+                    mass += c.y;
+                }
+            }
         }
     }
 
