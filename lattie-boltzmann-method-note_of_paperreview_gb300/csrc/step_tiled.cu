@@ -172,6 +172,7 @@ struct TiledKernel {
     struct Scal { float f6, f12, rho_mod, tau, lesC; };
     const S *__restrict__ fo;
     S *__restrict__ fn;
+    S *fnq[19];                // fn + q*N: per-direction bases, so a store is base + 32-bit node index
     Tables<float> T;
     StepConst k;
     TiledConst tc;
@@ -221,7 +222,7 @@ struct TiledKernel {
         float rho_s, u1, v1, w1;
         collide_node_pairs<LES>(Fl, sc.rho_mod, sc.f6, sc.f12, sc.tau, sc.lesC, rho_s, u1, v1, w1);
 #pragma unroll
-        for (int q = 0; q < 19; q++) store_f<S>(fn + (size_t)q*N, node, q, Fl[q]);
+        for (int q = 0; q < 19; q++) store_f<S>(fnq[q], (unsigned)node, q, Fl[q]);
         if (macros_on) { rho_out[node] = rho_s; u_out[node] = u1; v_out[node] = v1; w_out[node] = w1; }
         // column partials in FP32 (at most NZ terms), folded into FP64 once per column
         if (y == k.yplane) ub += v1*T.dxf[x]*T.dzf[z];
@@ -580,6 +581,8 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
             const unsigned long long st = step_s;
             K.fo = descs[w.x].buf[st & 1ULL];
             K.fn = descs[w.x].buf[(st + 1) & 1ULL];
+            const size_t N = (size_t)K.k.NX*K.k.NY*K.k.NZ;
+            for (int q = 0; q < 19; q++) K.fnq[q] = K.fn + q*N;
             K.tc.n = st + 1;
             K.mass_on = K.k.mass_interval > 0 && ((st + 1) % (unsigned long long)K.k.mass_interval) == 0ULL;
             K.macros_on = macros_on;
@@ -611,6 +614,7 @@ cudaError_t launch_t(const StepLaunch &L) {
     TiledKernel<S, LES, NXC> K;
     K.fo = (const S *)L.fo;
     K.fn = (S *)L.fn;
+    for (int q = 0; q < 19; q++) K.fnq[q] = K.fn + (size_t)q*L.k.NX*L.k.NY*L.k.NZ;
     K.T = *(const Tables<float> *)L.tables;
     K.k = L.k;
     K.tc = *(const TiledConst *)L.tiled;
