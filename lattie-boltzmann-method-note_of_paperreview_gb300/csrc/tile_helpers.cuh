@@ -48,8 +48,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
 // Bounded wait: gives up after about a second, records the fault and lets the kernel run
 // to its end (no thread can be left behind at a barrier). Returns whether the phase completed.
 // After one timeout the thread stops waiting altogether (`faulted`), so a broken pipeline
-// costs one bounded wait, not one per plane; warp 0 then starts no further copies and, at
-// the end of the kernel, waits (bounded again) for the copies it had started.
+// costs one bounded wait, not one per plane; the CTA then starts no further copies and, at the
+// end of the kernel, thread 0 waits (bounded again) for the copy phases still pending.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, Ctrl *ctrl, bool &faulted) {
     if (faulted) return false;
     for (int it = 0; it < (1 << 22); ++it) {
@@ -62,7 +62,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, Ctrl *
 }
 
 // Pipeline word kept by every thread: bit s = parity of the next completion of stage s;
-// bit PEND + s = warp 0 started a copy on stage s that it has not seen complete;
+// bit PEND + s = (thread 0) a copy phase was posted on stage s and not yet seen complete;
 // bit PPAR + s = the completion parity of that copy.
 constexpr int PEND = 8, PPAR = 16;
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
