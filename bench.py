@@ -49,14 +49,16 @@ def measured_peak_gbs():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clocks/throttle reasons sampled every 20 ms; the summary keeps the samples taken
+    between mark_start() and mark_end() (the timed region), by their timestamps."""
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, device):
         self.device = device
         self.proc = None
+        self.t0 = self.t1 = None
         self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
@@ -64,11 +66,21 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                          "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
+            # wait (at most 5 s) until the sampler is running, so the timed region is covered
+            deadline = time.time() + 5.0
+            while time.time() < deadline and os.path.getsize(self.path) == 0:
+                time.sleep(0.05)
         except Exception:
             self.proc = None
         return self
+
+    def mark_start(self):
+        self.t0 = time.time()
+
+    def mark_end(self):
+        self.t1 = time.time()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -80,16 +92,30 @@ class ClockSampler:
             self.fh.close()
 
     def summary(self):
+        import datetime
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         rows = []
         try:
             for line in open(self.path):
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
+                if len(parts) >= 10:
+                    try:
+                        t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    except ValueError:
+                        t = None
+                    rows.append((t, parts[1:]))
         except Exception:
             pass
+        window = "timed region"
+        if self.t0 is not None and self.t1 is not None:
+            inside = [r for t, r in rows if t is not None and self.t0 <= t <= self.t1]
+            if not inside:   # shorter than the sampling interval: the samples next to it
+                window = "within 50 ms of the timed region"
+                inside = [r for t, r in rows if t is not None and self.t0 - 0.05 <= t <= self.t1 + 0.05]
+            rows = inside
+        else:
+            rows = [r for _, r in rows]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
@@ -97,7 +123,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(rows), "window": window}
 
 
 def dist_env():
@@ -119,12 +145,16 @@ def time_steps(islbm, torch, solver, steps):
     return ev0.elapsed_time(ev1)
 
 
-def device_run(islbm, torch, precision, steps, warmup, device):
+def device_run(islbm, torch, precision, steps, warmup, device, clk=None):
     p = islbm.default_params(precision=precision, device=device, **CASE)
     with islbm.Solver(p) as s:
         s.step(warmup)
         s.sync()
+        if clk is not None:
+            clk.mark_start()
         ms = time_steps(islbm, torch, s, steps)
+        if clk is not None:
+            clk.mark_end()
         ok = s.healthy()
         fields = s.fields()
     n = CASE["NX"] * CASE["NY"] * CASE["NZ"]
@@ -334,7 +364,7 @@ def main():
     # plain FP32, device resident
     barrier()
     with ClockSampler(local) as clk:
-        r32 = device_run(islbm, torch, "fp32", args.steps, args.warmup, local)
+        r32 = device_run(islbm, torch, "fp32", args.steps, args.warmup, local, clk)
     barrier()
     ms = slowest_rank_ms(r32["ms"], world, "cuda")
     value = n * args.steps * world / (ms * 1e-3) / 1e6
