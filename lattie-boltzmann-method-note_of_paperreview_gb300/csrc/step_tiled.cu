@@ -116,8 +116,9 @@ __device__ __forceinline__ int r12_col(int p) { return 112 + 2*(p & 7); }
 
 // xi combination of the window of planes b .. b+6 held in the TMEM ring (`tl` = this warp's
 // lane-quarter address, `sb` = b mod 7). The 64 weights of (y, z) are interleaved per stencil point c:
-// (xi3, xi4, xi5, xi6, xi15, xi16, xi17, xi18)[c]. Writes F[3..18].
-__device__ __forceinline__ void xi_combine(uint32_t tl, int sb, const float *wv_, float *F) {
+// (xi3, xi4, xi5, xi6, xi15, xi16, xi17, xi18)[c]. Writes F[3..18], and F[1], F[2] from the
+// delay-line columns r12c.
+__device__ __forceinline__ void xi_combine(uint32_t tl, int sb, int r12c, const float *wv_, float *F) {
     const float4 *wv = (const float4 *)wv_;
     P2 a34 = p2(0.f, 0.f), a56 = a34, a1516 = a34, a1718 = a34, a79 = a34, a810 = a34, a1113 = a34, a1214 = a34;
     auto acc = [&](const uint32_t (&q)[16], int c) {
@@ -134,16 +135,22 @@ __device__ __forceinline__ void xi_combine(uint32_t tl, int sb, const float *wv_
     };
 #pragma unroll
     for (int c = 0; c < 6; c += 2) {
-        uint32_t q0[16], q1[16];
+        uint32_t q0[16], q1[16], r[2];
         const int s0 = sb + c, s1 = sb + c + 1;
         tmem_ld16(tl + ring_col(s0 >= 7 ? s0 - 7 : s0), q0);
         tmem_ld16(tl + ring_col(s1 >= 7 ? s1 - 7 : s1), q1);
+        if (c == 0) tmem_ld2(tl + r12c, r);   // F1, F2 of the target plane ride with the first pair
         tmem_wait_ld(q0, q1);
+        if (c == 0) {
+            tmem_tie(r);
+            F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
+        }
         acc(q0, c);
         acc(q1, c + 1);
     }
-    {
+    {   // the newest plane: its ring stores were issued by this thread just before
         uint32_t q0[16];
+        tmem_wait_st();
         tmem_ld16(tl + ring_col(sb == 0 ? 6 : sb - 1), q0);
         tmem_wait_ld(q0);
         acc(q0, 6);
@@ -377,15 +384,8 @@ struct TiledKernel {
                                            const Scal &sc, float &ub, float &mass) const {
         constexpr int NX = LY::NX;
         float F[19];
-        tmem_wait_st();   // this thread's ring stores of plane p are complete
         // window base p - 6 sits in slot (sp + 1) mod 7
-        xi_combine(tl, sp == 6 ? 0 : sp + 1, (const float *)(stage + LY::w_off) + yl*64, F);
-        {
-            uint32_t r[2];
-            tmem_ld2(tl + r12_col(t), r);
-            tmem_wait_ld(r);
-            F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
-        }
+        xi_combine(tl, sp == 6 ? 0 : sp + 1, r12_col(t), (const float *)(stage + LY::w_off) + yl*64, F);
         F[0] = ld1<S>((const S *)(stage + LY::f0_off) + yl*NX + x, (float)dev_ref(0));
         finish<false>(F, x, y, t, sc, ub, mass);
     }
@@ -395,14 +395,7 @@ struct TiledKernel {
     // loop's code stays small; returns the target's (ub, mass) contributions.
     __device__ __noinline__ float2 cap_target(uint32_t tl, int sp, int t, int x, int y, const Scal &sc) const {
         float F[19];
-        tmem_wait_st();
-        xi_combine(tl, sp == 6 ? 0 : sp + 1, T.wxi + ((size_t)t*k.NY + y)*64, F);
-        {
-            uint32_t r[2];
-            tmem_ld2(tl + r12_col(t), r);
-            tmem_wait_ld(r);
-            F[1] = __uint_as_float(r[0]); F[2] = __uint_as_float(r[1]);
-        }
+        xi_combine(tl, sp == 6 ? 0 : sp + 1, r12_col(t), T.wxi + ((size_t)t*k.NY + y)*64, F);
         F[0] = load_f<S>(fo, ((size_t)t*k.NY + y)*LY::NX + x, 0);
         float ub = 0.f, mass = 0.f;
         finish<true>(F, x, y, t, sc, ub, mass);

@@ -133,6 +133,12 @@ __device__ __forceinline__ void tmem_wait_ld(uint32_t (&a)[16]) {
                  :
                  : "memory");
 }
+// ties registers loaded before a tied wait: each empty volatile statement stays after that wait
+// and redefines its register, so no use of it is scheduled earlier
+template <int N> __device__ __forceinline__ void tmem_tie(uint32_t (&v)[N]) {
+#pragma unroll
+    for (int i = 0; i < N; i++) asm volatile("" : "+r"(v[i]));
+}
 __device__ __forceinline__ void tmem_wait_ld(uint32_t (&a)[2]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(a[0]), "+r"(a[1]) : : "memory");
 }
