@@ -40,8 +40,7 @@ template <int NXC> constexpr int threads_for() { return NXC < 128 ? 128 : NXC; }
 // TMEM columns of a CTA's xi ring: 128 per 128 threads (each thread's lane holds 126 values),
 // rounded up to a power of two as the allocator requires
 template <int NT> constexpr int ring_cols_for() { return NT <= 128 ? 128 : (NT <= 256 ? 256 : 512); }
-// Copy stages per tile: the next plane is in flight while one is filtered (a third stage for
-// the 2-byte formats, which would fit, measured no faster on GB300).
+// Copy stages per tile: the next plane's copies are in flight while one plane is filtered.
 template <class S> constexpr int stages_for() { return 2; }
 
 // Shared-memory layout of one tile for a spanwise width NXC (a power of two): all offsets are
@@ -678,9 +677,6 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
     TiledConst tc;
     std::memset(&tc, 0, sizeof(tc));
     tc.TY = k.NX < 128 ? 128/k.NX : 1;
-    int l = 0;
-    while ((1 << l) < k.NX) l++;
-    tc.log2nx = l;
     size_t smem;
     int ctas_tmem;
     if (precision == ISLBM_FP32) { const auto li = lay_for<float>(k.NX); smem = li.smem; ctas_tmem = li.ctas_per_sm; }
@@ -691,7 +687,6 @@ int make_tiled_const(const StepConst &k, int precision, const double *wx0, const
         tc.wy[a] = make_float2((float)wy0[a], (float)wy2[a]);
     }
     const int tiles = k.NY/tc.TY;
-    tc.units = (long long)tiles*k.NZ;
     // persistent CTAs: as many as fit on the SMs by shared memory (228 KB per SM, 1 KB reserved
     // per CTA) and by the TMEM rings (512 columns per SM; also the register bound of the kernel)
     const int per_sm = (int)std::min<size_t>((size_t)ctas_tmem, (228*1024)/(tc.smem_bytes + 1024));

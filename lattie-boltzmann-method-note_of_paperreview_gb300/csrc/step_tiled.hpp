@@ -10,11 +10,9 @@
 namespace islbm {
 
 struct TiledConst {
-    int TY;                       // streamwise rows per tile (256 / NX)
+    int TY;                       // streamwise rows per tile (128 / NX, 1 for NX >= 128)
     int grid;                     // persistent CTAs
     int zsegs;                    // wall-normal segments per column (work items = tiles * zsegs)
-    long long units;              // tiles * NZ (flattened work)
-    int log2nx;
     size_t smem_bytes;            // dynamic shared memory per CTA (layout: Lay in step_tiled.cu)
     // uniform-spacing Lagrange weights as (departure - minSize, departure + minSize) pairs, the
     // operand layout of the packed FP32x2 filters: wx[a] = (wx0[a], wx2[a]), wy[b] = (wy0[b], wy2[b])
