@@ -108,7 +108,7 @@ struct Group {
     bool les = false;
     std::vector<Solve *> members;
     void *descs = nullptr;       // device descriptors
-    int2 *items = nullptr;       // device (solve, tile) work list
+    int2 *items = nullptr;       // device (solve, segment*ntiles + tile) work list
     int nitems = 0;
     long long nodes = 0;         // lattice nodes updated per step
     int grid = 0;

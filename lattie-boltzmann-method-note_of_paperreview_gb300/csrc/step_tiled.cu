@@ -523,10 +523,10 @@ struct TiledKernel {
 };
 
 // Batched form: one launch advances every solve of a batch (same storage format and spanwise
-// width) by one step. Work items are (solve, tile) pairs; a CTA copies the solve's
+// width) by one step. Work items are (solve, segment*ntiles + tile) pairs; a CTA copies the solve's
 // descriptor into shared memory, takes the old/new buffers from the solve's own step
 // counter (so a graph of identical launches advances the solves step after step), runs the
-// column and reports it to the solve's controller, whose last column closes the step.
+// piece and reports it to the solve's controller, whose last piece closes the step.
 template <class S, bool LES, int NXC>
 struct BatchDesc {
     TiledKernel<S, LES, NXC> K;
@@ -560,7 +560,7 @@ step_tiled_batch_kernel(const BatchDesc<S, LES, NXC> *__restrict__ descs, const 
     unsigned parity = 0;
     bool faulted = false;
     for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-        const int2 w = items[it];   // (solve, tile)
+        const int2 w = items[it];   // (solve, segment*ntiles + tile)
         __syncthreads();            // previous item done with K and every stage
         {
             const unsigned *src = (const unsigned *)&descs[w.x].K;
