@@ -232,7 +232,7 @@ def cpu_oracle_run(steps, threads):
     return n * steps / dt / 1e6, dt
 
 
-def accuracy_run(islbm, device, steps=200):
+def accuracy_run(islbm, device, steps=1000):
     """Storage-format errors on the benchmark grid at a relaxation time where the reference
     scheme is stable (tau = 1.0; at Re_h 2800 it diverges): FP32 / FP16 / BF16 against FP64
     after `steps` steps from the same seeded state, and the total-mass drift of each."""
