@@ -24,6 +24,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -59,11 +60,11 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.t0 = self.t1 = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_%d.csv" % os.getpid())
+        fd, self.path = tempfile.mkstemp(prefix="islbm_clocks_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "20"], stdout=self.fh,
@@ -90,6 +91,12 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
             self.fh.close()
+
+    def __del__(self):
+        try:
+            os.unlink(self.path)
+        except Exception:
+            pass
 
     def summary(self):
         import datetime
@@ -218,12 +225,14 @@ def e2e_run(islbm, precision, steps, device, f_host):
                                                        "islbm_step / islbm_fields"}
 
 
-def cpu_oracle_run(steps, threads):
-    """The CPU oracle (reference restatement) on the same workload; returns MLUPS."""
+def cpu_oracle_run(steps, threads, warmup=1):
+    """The CPU oracle (reference restatement) on the same workload: `warmup` untimed steps, then
+    `steps` timed steps; returns (MLUPS, seconds of the timed steps)."""
     from oracle.oracle import Oracle
     o = Oracle(CASE["NX"], CASE["NY"], CASE["NZ"], re=CASE["Re"], ub=CASE["Uref"], ndtfrc=CASE["NDTFRC"],
                les_cs=CASE["les_cs"], threads=threads)
-    o.step(1)  # warm
+    if warmup > 0:
+        o.step(warmup)
     t0 = time.perf_counter()
     o.step(steps)
     dt = time.perf_counter() - t0
@@ -330,16 +339,22 @@ def main():
             return 0
         from oracle import build as ob
         ob.build()
-        # bounded sample: at most 12 full steps of the workload (about a minute on 16 cores)
-        cpu_steps = max(1, min(args.steps, 12))
-        mlups, dt = cpu_oracle_run(cpu_steps, threads)
+        # every step is a full step of the workload (about 0.7 s on 16 host cores): at most 100
+        # timed steps and 10 warm-up steps, and the line reports the counts actually run
+        cpu_steps = max(1, min(args.steps, 100))
+        cpu_warm = max(0, min(args.warmup, 10))
+        mlups, dt = cpu_oracle_run(cpu_steps, threads, warmup=cpu_warm)
         line = {"metric": METRIC, "value": mlups, "unit": "MLUPS", "impl": "reference", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / cpu_steps * 1e3,
+                "steps": cpu_steps, "warmup": cpu_warm, "ms_per_step": dt / cpu_steps * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic", "config": {"workload": WORKLOAD, "grid": "NY256 NX128 NZ192", "precision": "fp64"},
                 "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
-                                 "sample": f"{cpu_steps} steps of the full 256x128x192 grid, FP64, LES"},
+                                 "steps": cpu_steps, "warmup": cpu_warm, "seconds": dt,
+                                 "sample": f"{cpu_steps} full steps of the 256x128x192 grid after {cpu_warm} warm-up "
+                                           f"steps, FP64, LES, OpenMP over {threads} host threads"},
                 "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if cpu_steps != args.steps or cpu_warm != args.warmup:
+            line["requested"] = {"steps": args.steps, "warmup": args.warmup}
         print(json.dumps(line))
         return 0
 
@@ -401,8 +416,9 @@ def main():
         ob.build()
         mlups, dt = cpu_oracle_run(args.cpu_steps, threads)
         line["cpu_baseline"] = {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
-                                "sample": f"{args.cpu_steps} steps of the full 256x128x192 grid, FP64, LES",
-                                "seconds": dt}
+                                "steps": args.cpu_steps, "warmup": 1, "seconds": dt,
+                                "sample": f"{args.cpu_steps} full steps of the 256x128x192 grid after 1 warm-up step, "
+                                          f"FP64, LES, OpenMP over {threads} host threads"}
     if rank == 0 and not args.no_large:
         line["large"] = large_run(islbm, torch, local)
     if rank == 0 and not args.no_serve:

@@ -64,7 +64,9 @@ typedef enum islbm_layout {
 typedef enum islbm_kernel {
     ISLBM_KERNEL_AUTO = 0,       /* tiled kernel when the grid allows it, else gather kernel */
     ISLBM_KERNEL_GATHER = 1,     /* one thread per node, stencils read through L1/L2 */
-    ISLBM_KERNEL_TILED = 2       /* z-marching x-y tiles staged in shared memory */
+    ISLBM_KERNEL_TILED = 2,      /* z-marching x-y tiles staged in shared memory (two nodes per
+                                    thread where the width allows it, else one) */
+    ISLBM_KERNEL_TILED_SINGLE = 3 /* the tiled kernel with one node per thread */
 } islbm_kernel;
 
 /* Parameter set of C/variables.h (same names where the reference has one). */
@@ -201,12 +203,24 @@ ISLBM_API int islbm_stats_profile(islbm_handle *h, int quantity, int y, double *
  * below the first node, where the half-way bounce-back puts it) and the two lowest nodes. */
 ISLBM_API int islbm_stats_wall_shear(islbm_handle *h, double *cf);
 
+/* Statistics files of the reference, so that the time means survive a restart (Launch_OutputTB
+ * and InitialTBUsingBkpData, C/fileIO.h:356-500): <dir>/accu.dat holds the sample count, and the
+ * running sum of each quantity is <dir>/<NAME>/<NAME>_<rank>.bin (NAME = U, V, W, P, UU, ...,
+ * WWW, DUDX2, ... as islbm_stat), raw FP64 over k = 3..NZ6-4, j = 3..NYD6-4, i = 3..NX6-4 of the
+ * padded layout, k outermost. Write creates the per-quantity directories inside `dir` (which
+ * must exist); read replaces the current sums and sample count (gradient quantities are read
+ * when islbm_stats_gradients is on). */
+ISLBM_API int islbm_stats_write(islbm_handle *h, const char *dir, int rank);
+ISLBM_API int islbm_stats_read(islbm_handle *h, const char *dir, int rank);
+
 /* Checkpoint / restart in the reference's files (OutputData / InitialUsingBkpData,
  * C/fileIO.h:52-67, 262-266, 298-354): <dir>/{rho,u,v,w,f0..f18}_<rank>.bin as raw FP64 arrays
  * of NX6*NZ6*NYD6 values in the padded layout, and the body force as text in <dir>/0_force.dat.
  * The controller state (force, bulk-velocity window, step counter) is also written to
  * <dir>/islbm_ctrl_<rank>.bin; read uses it when present (exact resume) and otherwise the text
- * force, as the reference does. The directory must exist. */
+ * force, as the reference does. The directory must exist. When statistics are being accumulated,
+ * write also stores them with islbm_stats_write in <dir>/statistics (created), and read restores
+ * them from there when <dir>/statistics/accu.dat exists, so the time means continue exactly. */
 ISLBM_API int islbm_checkpoint_write(islbm_handle *h, const char *dir, int rank);
 ISLBM_API int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank);
 

@@ -52,13 +52,14 @@ size_t compute_bytes(int precision) { return precision == ISLBM_FP64 ? 8 : 4; }
 
 // table sizes in compute-type elements
 struct TabSizes {
-    size_t wx, wy, wxi, bq, bw, flags_bytes, dxv, dzv;
+    size_t wx, wy, wxi, wxi2, bq, bw, flags_bytes, dxv, dzv;
 };
 TabSizes tab_sizes(const islbm_params &p) {
     TabSizes s{};
     const size_t nb = 2*(size_t)(p.NY + 7);
     s.wx = 7*(size_t)p.NX; s.wy = 7*(size_t)p.NY;
     s.wxi = (size_t)p.NZ*p.NY*64;
+    s.wxi2 = p.precision == ISLBM_FP64 ? 0 : (size_t)p.NZ*p.NY*128;
     s.bq = 4*nb; s.bw = (size_t)Geometry::NBFL*7*nb;
     s.flags_bytes = 4*nb*sizeof(int);
     s.dxv = (size_t)p.NX; s.dzv = (size_t)p.NZ;
@@ -68,7 +69,7 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 size_t tables_bytes(const islbm_params &p) {
     const TabSizes s = tab_sizes(p);
     const size_t c = compute_bytes(p.precision);
-    return align256(2*s.wx*c) + align256(2*s.wy*c) + align256(s.wxi*c) + align256(s.bq*c) + align256(s.bw*c) +
+    return align256(2*s.wx*c) + align256(2*s.wy*c) + align256(s.wxi*c) + align256(s.wxi2*c) + align256(s.bq*c) + align256(s.bw*c) +
            align256(s.flags_bytes) + align256(s.dxv*8) + align256(s.dzv*8) + align256(s.dxv*4) + align256(s.dzv*4);
 }
 
@@ -112,6 +113,16 @@ void pack_tables(const Geometry &g, const islbm_params &p, std::vector<char> &bl
                 for (int a = 0; a < 7; a++)
                     wxi[((size_t)z*NY + y)*64 + a*8 + tt] = (C)g.XiT[((size_t)tt*7 + a)*nyz + (size_t)(y + 3)*NZ6 + (z + 3)];
     t.wxi = (const C *)dxi;
+    auto [hxi2, dxi2] = take(s.wxi2*sizeof(C));
+    C *wxi2 = (C *)hxi2;
+    for (size_t r = 0; r < s.wxi2/128; r++)
+        for (int a = 0; a < 8; a++)
+            for (int tt = 0; tt < 8; tt++) {
+                const C v = a < 7 ? wxi[r*64 + a*8 + tt] : (C)0;
+                wxi2[r*128 + a*16 + 2*tt] = v;
+                wxi2[r*128 + a*16 + 2*tt + 1] = v;
+            }
+    t.wxi2 = s.wxi2 ? (const C *)dxi2 : nullptr;
     auto [hq, dq] = take(s.bq*sizeof(C));
     for (size_t i = 0; i < s.bq; i++) ((C *)hq)[i] = (C)g.Q[i];
     t.bfl_q = (const C *)dq;
@@ -420,19 +431,23 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
     h->cur = 0;
     h->steps = 0;
     h->use_tiled = false;
-    if (p.kernel == ISLBM_KERNEL_TILED || p.kernel == ISLBM_KERNEL_AUTO) {
-        h->use_tiled = tiled_supported(k, p.precision);
-        if (h->use_tiled) {
-            int sms = 0;
-            CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-            double wx0[7], wx2[7], wy0[7], wy2[7];
-            for (int a = 0; a < 7; a++) {   // uniform spacing: the weights of the first node serve all
-                wx0[a] = h->g.XP0[(size_t)a*h->g.NX6 + 3]; wx2[a] = h->g.XP2[(size_t)a*h->g.NX6 + 3];
-                wy0[a] = h->g.YP0[(size_t)a*h->g.NYD6 + 3]; wy2[a] = h->g.YP2[(size_t)a*h->g.NYD6 + 3];
-            }
-            if (make_tiled_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) != 0) h->use_tiled = false;
+    h->paired = false;
+    if (p.kernel == ISLBM_KERNEL_TILED || p.kernel == ISLBM_KERNEL_AUTO || p.kernel == ISLBM_KERNEL_TILED_SINGLE) {
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+        double wx0[7], wx2[7], wy0[7], wy2[7];
+        for (int a = 0; a < 7; a++) {   // uniform spacing: the weights of the first node serve all
+            wx0[a] = h->g.XP0[(size_t)a*h->g.NX6 + 3]; wx2[a] = h->g.XP2[(size_t)a*h->g.NX6 + 3];
+            wy0[a] = h->g.YP0[(size_t)a*h->g.NYD6 + 3]; wy2[a] = h->g.YP2[(size_t)a*h->g.NYD6 + 3];
         }
-        if (p.kernel == ISLBM_KERNEL_TILED && !h->use_tiled) { g_last = "tiled kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
+        // the paired-node kernel where the grid allows it, else the one-node-per-thread kernel
+        if (p.kernel != ISLBM_KERNEL_TILED_SINGLE && pair_supported(k, p.precision) &&
+            make_pair_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) == 0) {
+            h->use_tiled = h->paired = true;
+        } else if (tiled_supported(k, p.precision) && make_tiled_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) == 0) {
+            h->use_tiled = true;
+        }
+        if (p.kernel != ISLBM_KERNEL_AUTO && !h->use_tiled) { g_last = "tiled kernel does not support this grid"; return ISLBM_ERR_NOT_SUPPORTED; }
     }
     CK(cudaStreamSynchronize(h->stream));
     return ISLBM_OK;
@@ -509,7 +524,7 @@ int islbm_step(islbm_handle *h, int nsteps) {
         L.mass = h->p.mass_interval > 0 && (n % (unsigned long long)h->p.mass_interval) == 0ULL;
         L.macros_on = (s == nsteps - 1);
         for (int m = 0; m < 4; m++) L.macros[m] = h->macros[m];
-        cudaError_t e = h->use_tiled ? launch_step_tiled(L) : launch_step_gather(L);
+        cudaError_t e = h->paired ? launch_step_pair(L) : h->use_tiled ? launch_step_tiled(L) : launch_step_gather(L);
         if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
         h->cur = 1 - h->cur;
         h->steps = n;

@@ -7,6 +7,9 @@
 // of either code can be resumed by the other. The text force keeps 15 decimals; to resume a run
 // of this library exactly, the controller state (force, bulk-velocity window, step counter) is
 // also written as <dir>/islbm_ctrl_<rank>.bin and used when present.
+#include <sys/stat.h>
+
+#include <cerrno>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -90,7 +93,22 @@ int islbm_checkpoint_write(islbm_handle *h, const char *dir, int rank) {
     if (!fp) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot write " + cpath).c_str());
     const size_t w = std::fwrite(&cf, sizeof(cf), 1, fp);
     if (std::fclose(fp) != 0 || w != 1) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("short write " + cpath).c_str());
+    if (h->stats) {   // the running statistics, in the reference's statistics files
+        const std::string sdir = std::string(dir) + "/statistics";
+        if (mkdir(sdir.c_str(), 0755) != 0 && errno != EEXIST)
+            return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot create " + sdir).c_str());
+        return islbm_stats_write(h, sdir.c_str(), rank);
+    }
     return ISLBM_OK;
+}
+
+// statistics of a checkpoint, when it has them
+static int read_stats_if_present(islbm_handle *h, const char *dir, int rank) {
+    const std::string sdir = std::string(dir) + "/statistics";
+    FILE *fp = std::fopen((sdir + "/accu.dat").c_str(), "r");
+    if (!fp) return ISLBM_OK;
+    std::fclose(fp);
+    return islbm_stats_read(h, sdir.c_str(), rank);
 }
 
 int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank) {
@@ -143,7 +161,7 @@ int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank) {
             std::swap(h->fbuf[0], h->fbuf[1]);
             h->cur = (int)(h->steps & 1ULL);
         }
-        return ISLBM_OK;
+        return read_stats_if_present(h, dir, rank);
     }
     const std::string fpath = std::string(dir) + "/0_force.dat";
     fp = std::fopen(fpath.c_str(), "r");
@@ -152,7 +170,8 @@ int islbm_checkpoint_read(islbm_handle *h, const char *dir, int rank) {
     const int got = std::fscanf(fp, "%lf", &force);
     std::fclose(fp);
     if (got != 1) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("bad force file " + fpath).c_str());
-    return islbm_set_force(h, force);
+    st = islbm_set_force(h, force);
+    return st != ISLBM_OK ? st : read_stats_if_present(h, dir, rank);
 }
 
 }  // extern "C"

@@ -131,7 +131,10 @@ constexpr int DIAG_MAX_DEVICES = 64;
 static __device__ __align__(256) unsigned char g_diag_scratch[islbm::DIAG_NOALLOC_BYTES];
 
 // Device address of g_diag_scratch per device: in host code the symbol name is not a device
-// address, so it is looked up once per device, with that device current.
+// address, so it is looked up once per device, with that device current. The address is kept
+// for the life of the process; a call checks that it still names device memory of that device
+// (a host program that called cudaDeviceReset has a new context, in which the module and its
+// array are loaded again) and looks it up again when it does not.
 static std::mutex g_diag_mu;
 static unsigned char *g_diag_ptr[islbm::DIAG_MAX_DEVICES] = {};
 
@@ -170,6 +173,14 @@ extern "C" int islbm_diagnostics_noalloc(islbm_handle *h, double *out) {
     {
         // set-up on the first call on this device, with the device current
         std::lock_guard<std::mutex> lock(g_diag_mu);
+        if (g_diag_ptr[h->device]) {
+            cudaPointerAttributes a;
+            if (cudaPointerGetAttributes(&a, g_diag_ptr[h->device]) != cudaSuccess || a.type != cudaMemoryTypeDevice ||
+                a.device != h->device) {
+                (void)cudaGetLastError();
+                g_diag_ptr[h->device] = nullptr;
+            }
+        }
         if (!g_diag_ptr[h->device]) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_diag_scratch);

@@ -91,7 +91,7 @@ int validate(const islbm_params &p) {
     if (p.les_cs < 0 || !(p.alpha > 0) || p.init_mode < 0 || p.init_mode > 1) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.mass_interval < 0 || p.bfl_mode < 0 || p.bfl_mode > 1) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.geometry < 0 || p.geometry > 1) return ISLBM_ERR_INVALID_ARGUMENT;
-    if (p.kernel < ISLBM_KERNEL_AUTO || p.kernel > ISLBM_KERNEL_TILED) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (p.kernel < ISLBM_KERNEL_AUTO || p.kernel > ISLBM_KERNEL_TILED_SINGLE) return ISLBM_ERR_INVALID_ARGUMENT;
     if (p.alpha != 1.0 && p.LY < 2.0*kBreak[5]*p.alpha) return ISLBM_ERR_INVALID_ARGUMENT;
     return ISLBM_OK;
 }

@@ -28,7 +28,8 @@ struct islbm_handle {
     StepConst k{};
     int cur = 0;
     unsigned long long steps = 0;
-    bool use_tiled = false;
+    bool use_tiled = false;    // a tiled kernel (shared-memory tiles, TMEM ring) steps this solve
+    bool paired = false;       // ... the paired-node one (step_pair.cu), else step_tiled.cu
     double *stats = nullptr;   // time-average accumulators, ISLBM_STAT_COUNT x N (allocated on first use)
     long long stats_samples = 0;
     int stats_grad = 0;        // gradient quantities requested (ISLBM_STAT_ALL sums instead of COUNT)

@@ -106,6 +106,7 @@ struct Solve {
 struct Group {
     int precision = 0, NX = 0;
     bool les = false;
+    bool paired = false;         // members step with the paired-node kernel (step_pair.cu)
     std::vector<Solve *> members;
     void *descs = nullptr;       // device descriptors
     int2 *items = nullptr;       // device (solve, segment*ntiles + tile) work list
@@ -244,7 +245,7 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
         islbm_handle *h = v->h;
         if (!h->use_tiled) { singles.push_back(v); continue; }
         const std::string sig = std::to_string(h->p.precision) + "/" + std::to_string(h->p.NX) + "/" +
-                                std::to_string(h->p.les_cs > 0.0 ? 1 : 0);
+                                std::to_string(h->p.les_cs > 0.0 ? 1 : 0) + "/" + std::to_string(h->paired ? 1 : 0);
         by[sig].push_back(v);
     }
     for (auto &kv : by) {
@@ -255,10 +256,11 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
         if (it != s->groups.end()) { free_group(it->second.get()); s->groups.erase(it); }
         auto g = std::make_unique<Group>();
         islbm_handle *h0 = kv.second[0]->h;
-        g->precision = h0->p.precision; g->NX = h0->p.NX; g->les = h0->p.les_cs > 0.0;
+        g->precision = h0->p.precision; g->NX = h0->p.NX; g->les = h0->p.les_cs > 0.0; g->paired = h0->paired;
         g->members = kv.second;
         g->key = key;
-        const size_t db = batch_desc_bytes(g->precision, g->NX, g->les);
+        const size_t db = g->paired ? pair_batch_desc_bytes(g->precision, g->NX, g->les)
+                                    : batch_desc_bytes(g->precision, g->NX, g->les);
         std::vector<unsigned char> hd(db*g->members.size());
         std::vector<int2> items;
         int maxt = 0, total_tiles = 0, min_nz = 1 << 30;
@@ -271,11 +273,13 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
         }
         // wall-normal segments per column: enough work items for four CTAs per SM, each segment
         // at least 16 targets long (a segment re-reads the 6 planes below it to fill its ring)
-        const int nseg = std::max(1, std::min(4*s->sms/std::max(1, total_tiles), min_nz/16));
+        // (paired kernel: two CTAs per SM, segment count by the makespan estimate of pair_zsegs)
+        const int nseg = g->paired ? pair_zsegs(total_tiles, 2*s->sms, min_nz)
+                                   : std::max(1, std::min(4*s->sms/std::max(1, total_tiles), min_nz/16));
         for (size_t m = 0; m < g->members.size(); m++) {
             islbm_handle *h = g->members[m]->h;
             g->nodes += (long long)h->N;
-            fill_batch_desc(g->precision, g->NX, g->les, h->tf, h->k, h->tiled, h->ctrl, h->macros, h->fbuf[0], h->fbuf[1],
+            (g->paired ? fill_pair_batch_desc : fill_batch_desc)(g->precision, g->NX, g->les, h->tf, h->k, h->tiled, h->ctrl, h->macros, h->fbuf[0], h->fbuf[1],
                             h->p.NY/h->tiled.TY, nseg, hd.data() + m*db);
         }
         // segment-major, the solves' tiles interleaved, so that neighbouring tiles of a solve at
@@ -306,6 +310,12 @@ int build_groups(islbm_server *s, std::vector<Group *> &out, std::vector<Solve *
     return ISLBM_OK;
 }
 
+// one batched step of every member of g on the group's stream
+cudaError_t launch_batch(Group *g, int grid, int macros_on) {
+    return g->paired ? launch_step_pair_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, grid, macros_on, g->stream)
+                     : launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, grid, macros_on, g->stream);
+}
+
 // Autotuner: candidate persistent-CTA counts for a batch, timed on one real step each.
 // Returns a status; the timed launches advance every member and are accounted for here.
 int tune(islbm_server *s, Group *g) {
@@ -325,7 +335,7 @@ int tune(islbm_server *s, Group *g) {
     for (int c = 0; c < 3; c++) {
         if (c > 0 && cand[c] == cand[c - 1]) continue;
         SK(cudaEventRecord(e0, g->stream));
-        SK(launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, cand[c], 1, g->stream));
+        SK(launch_batch(g, cand[c], 1));
         SK(cudaEventRecord(e1, g->stream));
         SK(cudaEventSynchronize(e1));
         launched++;
@@ -346,11 +356,10 @@ int run_group_chunk(islbm_server *s, Group *g, int steps) {
         if (g->graph) cudaGraphExecDestroy(g->graph);
         g->graph = nullptr;
         cudaGraph_t graph;
-        SK(prepare_step_tiled_batch(g->precision, g->NX, g->les));
+        SK(g->paired ? prepare_step_pair_batch(g->precision, g->NX, g->les) : prepare_step_tiled_batch(g->precision, g->NX, g->les));
         SK(cudaStreamBeginCapture(g->stream, cudaStreamCaptureModeThreadLocal));
         for (int j = 0; j < steps; j++) {
-            cudaError_t e = launch_step_tiled_batch(g->precision, g->NX, g->les, g->descs, g->items, g->nitems, g->grid,
-                                                    j == steps - 1, g->stream);
+            cudaError_t e = launch_batch(g, g->grid, j == steps - 1);
             if (e != cudaSuccess) { cudaStreamEndCapture(g->stream, &graph); return fail(s, e, "batched step capture"); }
         }
         SK(cudaStreamEndCapture(g->stream, &graph));

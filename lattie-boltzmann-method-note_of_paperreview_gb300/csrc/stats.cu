@@ -6,9 +6,14 @@
 // last step (islbm_step writes them on its last step). The accumulators are one allocation of
 // 24*N doubles, laid out [quantity][z][y][x]; a sample reads 16 B (FP32 fields) or 32 B (FP64)
 // and updates 24 x 8 B per node, so it is HBM bound at about 400 B per node.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cerrno>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "handle.hpp"
@@ -256,6 +261,90 @@ int islbm_stats_wall_shear(islbm_handle *h, double *cf) {
         const double a = (ut[0]*d[1]*d[1] - ut[1]*d[0]*d[0])/(d[0]*d[1]*(d[1] - d[0]));
         cf[y] = 2.0*g.niu*a/(g.Uref*g.Uref);
     }
+    return ISLBM_OK;
+}
+
+
+// Statistics files of the reference (Launch_OutputTB / OutputTBData and InitialTBUsingBkpData /
+// ReadTBData, C/fileIO.h:356-500): <dir>/accu.dat holds the sample count as text ("%d"), and each
+// quantity's running sum is <dir>/<NAME>/<NAME>_<rank>.bin, raw FP64 in the order
+// k = 3..NZ6-4, j = 3..NYD6-4, i = 3..NX6-4 of the padded layout (NZ x (NY+1) x (NX+1) values:
+// the periodic end nodes j = NY+3, i = NX+3 are written as copies of j = 3, i = 3).
+static const char *const kStatNames[ISLBM_STAT_ALL] = {
+    "U", "V", "W", "P", "UU", "UV", "UW", "VV", "VW", "WW", "PU", "PV", "PW", "PP", "KT",
+    "UUU", "UUV", "UUW", "VVU", "VVV", "VVW", "WWU", "WWV", "WWW",
+    "DUDX2", "DUDY2", "DUDZ2", "DVDX2", "DVDY2", "DVDZ2", "DWDX2", "DWDY2", "DWDZ2"};
+
+static std::string tb_path(const char *dir, int q, int rank) {
+    return std::string(dir) + "/" + kStatNames[q] + "/" + kStatNames[q] + "_" + std::to_string(rank) + ".bin";
+}
+
+int islbm_stats_write(islbm_handle *h, const char *dir, int rank) {
+    if (!h || !dir) return ISLBM_ERR_INVALID_ARGUMENT;
+    if (!h->stats) return report_status(ISLBM_ERR_NOT_SUPPORTED, "no statistics to write (islbm_stats_reset first)");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return report_cuda(e, "cudaSetDevice");
+    const int NX = h->p.NX, NY = h->p.NY, NZ = h->p.NZ;
+    {
+        const std::string path = std::string(dir) + "/accu.dat";
+        FILE *fp = std::fopen(path.c_str(), "w");
+        if (!fp) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot write " + path).c_str());
+        std::fprintf(fp, "%lld", h->stats_samples);
+        if (std::fclose(fp) != 0) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot write " + path).c_str());
+    }
+    std::vector<double> sum(h->N), out((size_t)NZ*(NY + 1)*(NX + 1));
+    for (int q = 0; q < h->stats_nq; q++) {
+        e = cudaMemcpyAsync(sum.data(), h->stats + (size_t)q*h->N, h->N*sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return report_cuda(e, "statistics read");
+        size_t o = 0;
+        for (int z = 0; z < NZ; z++)
+            for (int j = 0; j <= NY; j++)
+                for (int i = 0; i <= NX; i++) out[o++] = sum[((size_t)z*NY + (j % NY))*NX + (i % NX)];
+        const std::string sub = std::string(dir) + "/" + kStatNames[q];
+        if (mkdir(sub.c_str(), 0755) != 0 && errno != EEXIST)
+            return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot create " + sub).c_str());
+        const std::string path = tb_path(dir, q, rank);
+        FILE *fp = std::fopen(path.c_str(), "wb");
+        if (!fp) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot write " + path).c_str());
+        const size_t w = std::fwrite(out.data(), sizeof(double), out.size(), fp);
+        if (std::fclose(fp) != 0 || w != out.size()) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("short write " + path).c_str());
+    }
+    return ISLBM_OK;
+}
+
+int islbm_stats_read(islbm_handle *h, const char *dir, int rank) {
+    if (!h || !dir) return ISLBM_ERR_INVALID_ARGUMENT;
+    long long samples = 0;
+    {
+        const std::string path = std::string(dir) + "/accu.dat";
+        FILE *fp = std::fopen(path.c_str(), "r");
+        if (!fp) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot read " + path).c_str());
+        const int got = std::fscanf(fp, "%lld", &samples);
+        std::fclose(fp);
+        if (got != 1 || samples < 0) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("bad sample count in " + path).c_str());
+    }
+    int st = islbm_stats_reset(h);   // allocates (gradients as enabled) and zeroes the sums
+    if (st != ISLBM_OK) return st;
+    const int NX = h->p.NX, NY = h->p.NY, NZ = h->p.NZ;
+    std::vector<double> in((size_t)NZ*(NY + 1)*(NX + 1)), sum(h->N);
+    for (int q = 0; q < h->stats_nq; q++) {
+        const std::string path = tb_path(dir, q, rank);
+        FILE *fp = std::fopen(path.c_str(), "rb");
+        if (!fp) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("cannot read " + path).c_str());
+        const size_t r = std::fread(in.data(), sizeof(double), in.size(), fp);
+        std::fclose(fp);
+        if (r != in.size()) return report_status(ISLBM_ERR_INVALID_ARGUMENT, ("short file " + path).c_str());
+        for (int z = 0; z < NZ; z++)
+            for (int j = 0; j < NY; j++)
+                for (int i = 0; i < NX; i++)
+                    sum[((size_t)z*NY + j)*NX + i] = in[((size_t)z*(NY + 1) + j)*(NX + 1) + i];
+        cudaError_t e = cudaMemcpyAsync(h->stats + (size_t)q*h->N, sum.data(), h->N*sizeof(double), cudaMemcpyHostToDevice,
+                                        h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) return report_cuda(e, "statistics upload");
+    }
+    h->stats_samples = samples;
     return ISLBM_OK;
 }
 

@@ -86,6 +86,8 @@ template <class C> struct Tables {
     const C *wx0, *wx2;        // [a*NX + x], departure x -/+ minSize
     const C *wy0, *wy2;        // [a*NY + y], departure y -/+ minSize
     const C *wxi;              // [(z*NY + y)*64 + a*8 + t]
+    const C *wxi2;             // the same as duplicated pairs, [(z*NY + y)*128 + a*16 + 2*t + {0, 1}]
+                               // (FP32 tables only; the paired-node kernel's operand layout)
     const int *bfl_flag;       // [t*nb + r], t: F3, F4, F15, F16; nb = 2*NYD6
     const C *bfl_q;            // [t*nb + r]
     const C *bfl_w;            // [(s*7 + a)*nb + r], s: XB37 XB38 YB378 XiB378 XB49 XB410 YB4910 XiB4910 YB15 XiB15 YB16 XiB16

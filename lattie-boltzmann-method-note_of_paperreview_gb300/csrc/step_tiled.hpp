@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "step_common.cuh"
+#include "step_launch.hpp"
 
 namespace islbm {
 
@@ -17,6 +18,11 @@ struct TiledConst {
     // uniform-spacing Lagrange weights as (departure - minSize, departure + minSize) pairs, the
     // operand layout of the packed FP32x2 filters: wx[a] = (wx0[a], wx2[a]), wy[b] = (wy0[b], wy2[b])
     float2 wx[7], wy[7];
+    // paired-node kernel (step_pair.cu): streamwise weights as broadcast pairs (wyb[0] = (wy0, wy0),
+    // wyb[1] = (wy2, wy2)) and the spanwise weights of aligned node pairs for node 0 (wxa) and
+    // node 1 (wxb), set 0 = wx0, set 1 = wx2
+    float2 wyb[2][7];
+    float2 wxa[2][4], wxb[2][4];
     unsigned long long n;         // step number (set per launch)
 };
 
@@ -32,5 +38,19 @@ void fill_batch_desc(int precision, int NX, bool les, const Tables<float> &T, co
 cudaError_t prepare_step_tiled_batch(int precision, int NX, bool les);
 cudaError_t launch_step_tiled_batch(int precision, int NX, bool les, const void *descs, const int2 *items, int nitems,
                                     int grid, int macros_on, cudaStream_t stream);
+
+// Paired-node tiled step (step_pair.cu): two spanwise-adjacent nodes per thread, packed FP32x2
+// arithmetic; same launch constants, the same batched interface.
+bool pair_supported(const StepConst &k, int precision);
+int make_pair_const(const StepConst &k, int precision, const double *wx0, const double *wx2, const double *wy0,
+                    const double *wy2, int num_sms, TiledConst *out);
+int pair_zsegs(int tiles, int slots, int NZ);
+cudaError_t launch_step_pair(const StepLaunch &L);
+size_t pair_batch_desc_bytes(int precision, int NX, bool les);
+void fill_pair_batch_desc(int precision, int NX, bool les, const Tables<float> &T, const StepConst &k, const TiledConst &tc,
+                          Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, int nseg, void *out);
+cudaError_t prepare_step_pair_batch(int precision, int NX, bool les);
+cudaError_t launch_step_pair_batch(int precision, int NX, bool les, const void *descs, const int2 *items, int nitems,
+                                   int grid, int macros_on, cudaStream_t stream);
 
 }  // namespace islbm

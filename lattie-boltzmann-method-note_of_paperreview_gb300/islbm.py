@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libislbm_gb300.so")
 FP64, FP32, FP16_DEV, BF16_DEV = 0, 1, 2, 3
 PRECISIONS = {"fp64": FP64, "fp32": FP32, "fp16": FP16_DEV, "bf16": BF16_DEV}
 LAYOUT_UNIQUE, LAYOUT_REFERENCE = 0, 1
-KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILED = 0, 1, 2
+KERNEL_AUTO, KERNEL_GATHER, KERNEL_TILED, KERNEL_TILED_SINGLE = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "HBM budget exceeded",
           5: "non-finite state", 6: "not supported", 7: "no CUDA device"}
@@ -114,6 +114,8 @@ def load():
         "islbm_stats_mean": [vp, ip, vp, ip],
         "islbm_stats_profile": [vp, ip, ip, vp],
         "islbm_stats_wall_shear": [vp, vp],
+        "islbm_stats_write": [vp, ctypes.c_char_p, ip],
+        "islbm_stats_read": [vp, ctypes.c_char_p, ip],
         "islbm_host_table": [P, ctypes.c_char_p, ip, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_host_table_int": [P, ctypes.c_char_p, vp, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)],
         "islbm_server_create": [ip, ctypes.c_size_t, ip, ctypes.POINTER(vp)],
@@ -297,6 +299,14 @@ class Solver:
 
     def checkpoint_read(self, directory, rank=0):
         check(self._L.islbm_checkpoint_read(self._h, os.fsencode(directory), int(rank)))
+
+    def stats_write(self, directory, rank=0):
+        """The running sums and sample count in the reference's statistics files (Launch_OutputTB)."""
+        check(self._L.islbm_stats_write(self._h, str(directory).encode(), rank))
+
+    def stats_read(self, directory, rank=0):
+        """Replace the running sums and sample count from statistics files (InitialTBUsingBkpData)."""
+        check(self._L.islbm_stats_read(self._h, str(directory).encode(), rank))
 
     def stats_reset(self):
         check(self._L.islbm_stats_reset(self._h))

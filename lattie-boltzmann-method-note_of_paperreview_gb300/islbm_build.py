@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libislbm_gb300.so")
-SOURCES = ["abi.cu", "geometry.cpp", "step_gather.cu", "step_tiled.cu", "serve.cu", "diagnostics.cu", "stats.cu", "checkpoint.cu", "writers.cu"]
+SOURCES = ["abi.cu", "geometry.cpp", "step_gather.cu", "step_tiled.cu", "step_pair.cu", "serve.cu", "diagnostics.cu", "stats.cu", "checkpoint.cu", "writers.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -88,3 +88,49 @@ def test_divergent_solve_retires(islbm_lib):
         assert srv.info(rg)["status"] == "capped"
         ref, _ = alone(islbm, good, 300)
         assert rel_l2(srv.fields(rg)["rho"], ref["rho"]) <= 1e-6
+
+
+def test_continuous_batching_admits_mid_flight(islbm_lib):
+    """Requests submitted between pumps while others are part-way through their solve: one joins
+    a running batch (new composition, new graph), one of a new width forms a new batch (graph
+    capture and tuning), one arrives after a retirement, and an FP64 solve runs alongside. Each
+    result equals the same parameters run alone, to the tolerances of the mixed test."""
+    islbm = islbm_lib
+    chunk = 50
+    spec = {   # name: (precision, NX, les_cs, tau, steps cap)
+        "a": ("fp32", 32, 0.0, 0.60, 300), "b": ("fp16", 32, 0.0, 0.62, 250), "c": ("fp32", 32, 0.1, 0.61, 200),
+        "d": ("fp32", 64, 0.0, 0.90, 150), "e": ("fp32", 32, 0.0, 0.64, 100), "f": ("fp32", 32, 0.0, 0.66, 150),
+        "g": ("fp64", 32, 0.0, 0.60, 100),
+    }
+    params = {}
+    for i, (k, (prec, nx, cs, tau, cap)) in enumerate(spec.items()):
+        params[k] = stable(islbm, NX=nx, NY=2 * nx, NZ=3 * nx // 2, tau=tau, precision=prec, les_cs=cs)
+        params[k].seed = 11 + i
+    ids = {}
+    with islbm.Server(steps_per_chunk=chunk) as srv:
+        def submit(*names):
+            for k in names:
+                ids[k] = srv.submit(params[k], max_steps=spec[k][4], tol=0.0, keep_fields=True)
+
+        submit("a", "e")
+        srv.pump()                        # a, e at one chunk
+        submit("b", "c")                  # join while a and e are part-way
+        srv.pump()
+        assert srv.info(ids["a"])["status"] == "active" and srv.info(ids["b"])["status"] == "active"
+        submit("d", "g")                  # a new width: its own batch, captured and tuned now
+        srv.pump()
+        while srv.info(ids["e"])["status"] == "active":
+            srv.pump()                    # e reaches its cap and retires
+        assert srv.info(ids["a"])["status"] == "active"
+        submit("f")                       # admitted after that retirement, into the running batch
+        srv.drain()
+        vel = lambda d: np.stack([d["u"], d["v"], d["w"]])
+        assert srv.info(ids["f"])["t_admit"] >= srv.info(ids["e"])["t_done"]
+        for k, (prec, nx, cs, tau, cap) in spec.items():
+            info = srv.info(ids[k])
+            assert info["status"] == "capped" and info["steps"] == cap, (k, info)
+            got = srv.fields(ids[k])
+            ref, force = alone(islbm, params[k], cap)
+            err_rho, err_u = rel_l2(got["rho"], ref["rho"]), rel_l2(vel(got), vel(ref))
+            assert err_rho <= TOL[prec] and err_u <= 10 * TOL[prec], (k, err_rho, err_u)
+            assert abs(info["force"] - force) <= 1e-6 * abs(force) + 1e-12, k
