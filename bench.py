@@ -193,6 +193,56 @@ def large_run(islbm, torch, device, steps=10, warmup=3):
     return out
 
 
+def large_accuracy_run(islbm, device, coarse_steps=300, samples=10):
+    """Accuracy of the large grid (768x384x512) against an FP64 run of the benchmark grid
+    (256x128x192): time-averaged u, v, w profiles at x/h = 0.5, 2, 4, 6, 8, the fine profiles
+    interpolated (linearly in the wall-normal coordinate) to the coarse nodes of the same column.
+    Both grids run the same physical case: U_b = 0.04, LES C_s = 0.1, and one Reynolds number at
+    which the reference scheme is stable on both (tau = 1.0 on the coarse grid, hence tau = 1.83
+    on the fine one); the same physical time (dt = minSize, so 8/3 fine steps per coarse step)
+    and the same sampling instants. The error is dominated by the grids' discretisation
+    difference; FP32 and FP16 storage are compared with the same coarse reference."""
+    import numpy as np
+    coarse = dict(NX=128, NY=256, NZ=192, Uref=0.04, NDTFRC=100, les_cs=0.1)
+    fine = dict(NX=384, NY=768, NZ=512, Uref=0.04, NDTFRC=100, les_cs=0.1)
+    ms_c = (3.036 - 1.0) / coarse["NZ"] * 0.6
+    re = 3.0 * coarse["Uref"] / (0.5 * ms_c)
+    ratio = fine["NZ"] / coarse["NZ"]                       # 8/3 fine steps per coarse step
+    every_c = coarse_steps // samples
+    every_f = int(round(every_c * ratio))
+    assert abs(every_f - every_c * ratio) < 1e-9
+    stations = [int(round(st * coarse["NY"] / 9.0)) % coarse["NY"] for st in (0.5, 2.0, 4.0, 6.0, 8.0)]
+    scale = fine["NY"] // coarse["NY"]                       # coarse row y is fine row 3y (same position)
+
+    def profiles(case, prec, every):
+        p = islbm.default_params(precision=prec, device=device, Re=re, **case)
+        z = islbm.host_table(p, "z").reshape(case["NY"] + 7, case["NZ"] + 6)
+        rows = stations if case is coarse else [scale * y for y in stations]
+        t0 = time.perf_counter()
+        with islbm.Solver(p) as s:
+            s.stats_reset()
+            for _ in range(samples):
+                s.step(every)
+                s.stats_accumulate()
+            prof = np.stack([[s.stats_profile(q, y) for y in rows] for q in ("U", "V", "W")])
+            healthy = s.healthy()
+        zc = np.stack([z[y + 3, 3:3 + case["NZ"]] for y in rows])
+        return prof, zc, healthy, time.perf_counter() - t0
+
+    ref, zref, ok_ref, _ = profiles(coarse, "fp64", every_c)
+    out = {"coarse": "256x128x192 FP64, %d steps, tau 1.0 (Re_h %.1f)" % (coarse_steps, re),
+           "fine": "768x384x512, %d steps, tau %.3f" % (every_f * samples, 0.5 + 0.5 * ratio),
+           "samples": samples, "stations_x_over_h": [0.5, 2, 4, 6, 8], "coarse_healthy": ok_ref}
+    for prec in ("fp32", "fp16"):
+        prof, zf, ok, tf = profiles(fine, prec, every_f)
+        err = 0.0
+        for c in range(3):
+            for i in range(len(stations)):
+                err = max(err, float(np.max(np.abs(np.interp(zref[i], zf[i], prof[c, i]) - ref[c, i]))))
+        out[prec] = {"time_avg_profiles_max_abs_err_over_ub": err / fine["Uref"], "healthy": ok, "seconds": tf}
+    return out
+
+
 def e2e_run(islbm, precision, steps, device, f_host):
     """Through the C ABI with host buffers: upload the state from pinned host memory, step, and
     read the fields into pinned host memory every 100 steps (the reference main loop's cadence)."""
@@ -404,6 +454,13 @@ def main():
             ach = 2 * 19 * 2 * n / (r["ms"] * 1e-3 / args.steps) / 1e9
             mixed[prec] = {"mlups": r["mlups"], "speedup_vs_fp32": r["mlups"] / r32["mlups"],
                            "hbm_gbs": ach, "frac": ach / peak, "steps": args.steps + args.warmup}
+        # the FP64 step on the same workload (config side by side with FP32): the one-thread-per-node
+        # kernel, bound by the FP64 pipe of GB300 rather than by memory
+        steps64 = max(1, min(args.steps, 20))
+        r = device_run(islbm, torch, "fp64", steps64, 2, local)
+        ach = 2 * 19 * 8 * n / (r["ms"] * 1e-3 / steps64) / 1e9
+        mixed["fp64"] = {"mlups": r["mlups"], "speedup_vs_fp32": r["mlups"] / r32["mlups"], "hbm_gbs": ach,
+                         "frac": ach / peak, "steps": steps64, "kernel": "one thread per node (FP64 parity path)"}
         line["mixed"] = mixed
         line["accuracy"] = accuracy_run(islbm, local)
     if rank == 0 and not args.no_e2e:
@@ -421,6 +478,7 @@ def main():
                                           f"FP64, LES, OpenMP over {threads} host threads"}
     if rank == 0 and not args.no_large:
         line["large"] = large_run(islbm, torch, local)
+        line["large"]["accuracy"] = large_accuracy_run(islbm, local)
     if rank == 0 and not args.no_serve:
         line["serve"] = serve_run(islbm, args.serve_requests, local)
     if rank == 0:

@@ -7,9 +7,9 @@
 //     x0 = 2*(thread % (NX/2)) and x0 + 1) and marches upward through a wall-normal segment of
 //     that column; each plane's 18 moving populations are copied global -> shared memory by
 //     cp.async.bulk (the ten with e_y != 0 with a 3-row streamwise halo on both sides, periodic
-//     wrap by splitting the copy), issued by lane 0 of four warps, a fixed quarter of the
-//     copies each: every operand is uniform over the issuing warp, so a copy costs a few uniform
-//     instructions and no warp carries the whole issue;
+//     wrap by splitting the copy), issued by one thread: every operand is uniform over the CTA,
+//     so a copy costs a few uniform instructions (spreading the copies over four warps was
+//     slower: every issuing warp then stalls right after the barrier);
 //   * front buffer (populations read before the plane's CTA barrier: the streamwise-filtered
 //     ten and the xi-only 5, 6) and stage buffer (1, 2, 11..14, read after it, plus the target
 //     row's xi weights and f0) have mbarriers of their own, so the front copies of plane p + 2
@@ -257,15 +257,12 @@ struct PairKernel {
 
     // Copies of plane p: the front part into front buffer f and/or the stage part (with the target
     // rows of plane p - 3 when that target is staged) into stage s. Called by every thread after a
-    // CTA barrier; lane 0 of warps 0..3 each issue a fixed quarter of the copies (job j on warp
-    // j mod 4), so every operand is uniform over the issuing warp and the issue work is spread.
-    // Thread 0 posts the expected bytes and keeps the pending record; a copy may complete before
-    // the bytes are posted (the phase cannot end while thread 0's arrival is due).
+    // CTA barrier; thread 0 issues every copy (its operands are uniform over the CTA), posting the
+    // expected bytes first and keeping the pending record for the drain.
     __device__ __forceinline__ void issue(unsigned char *smem, int p, int f, int s, bool do_front, bool do_stage,
                                           const Piece &P, unsigned &pipe, int tid) const {
         constexpr int NX = LY::NX, TY = LY::TY;
-        const int warp = tid >> 5;
-        if ((tid & 31) != 0 || warp >= 4) return;
+        if (tid != 0) return;
         if (*(volatile int *)(smem + LY::flag_off)) return;   // a wait timed out: no further copies
         if (p == k.drill_plane) return;                        // failure drill: this plane never arrives
         const int NY = k.NY;
@@ -276,17 +273,14 @@ struct PairKernel {
         fence_proxy_async();
         if (do_front) {
             uint64_t *bar = bars + f;
-            if (tid == 0) {
-                mbar_expect_tx(bar, LY::front_tx());
-                pipe = (pipe & ~(1u << (PPARF + f))) | (((pipe >> (FP + f)) & 1u) << (PPARF + f)) | (1u << (PENDF + f));
-            }
+            mbar_expect_tx(bar, LY::front_tx());
+            pipe = (pipe & ~(1u << (PPARF + f))) | (((pipe >> (FP + f)) & 1u) << (PPARF + f)) | (1u << (PENDF + f));
             unsigned char *dst = smem + LY::front_off(f);
             const int ys = P.y0 >= 3 ? P.y0 - 3 : P.y0 - 3 + NY;
             constexpr int rows = TY + 6;
             const int first = min(rows, NY - ys);
 #pragma unroll
             for (int i = 0; i < 10; i++) {
-                if ((i & 3) != warp) continue;
                 S *d = (S *)(dst + LY::fq_off_bytes(i));
                 const S *src = plane + (size_t)FQ(i)*N;
                 bulk_g2s(d, src + (size_t)ys*NX, first*row_bytes, bar);
@@ -294,25 +288,22 @@ struct PairKernel {
             }
 #pragma unroll
             for (int i = 10; i < 12; i++)
-                if ((i & 3) == warp)
-                    bulk_g2s(dst + LY::fq_off_bytes(i), plane + (size_t)FQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
+                bulk_g2s(dst + LY::fq_off_bytes(i), plane + (size_t)FQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
         }
         if (do_stage) {
             uint64_t *bar = bars + LY::NF + s;
             const int t = p - 3;
             const bool tgt = t >= 4 && t <= k.NZ - 4 && t >= P.ta && t < P.tb;
-            if (tid == 0) {
-                mbar_expect_tx(bar, LY::stage_tx + (tgt ? LY::tgt_tx : 0u));
-                pipe = (pipe & ~(1u << (PPARS + s))) | (((pipe >> (SP + s)) & 1u) << (PPARS + s)) | (1u << (PENDS + s));
-            }
+            mbar_expect_tx(bar, LY::stage_tx + (tgt ? LY::tgt_tx : 0u));
+            pipe = (pipe & ~(1u << (PPARS + s))) | (((pipe >> (SP + s)) & 1u) << (PPARS + s)) | (1u << (PENDS + s));
             unsigned char *dst = smem + LY::stage_off(s);
 #pragma unroll
             for (int i = 0; i < 6; i++)
-                if ((i & 3) == warp)
-                    bulk_g2s(dst + LY::sq_off_bytes(i), plane + (size_t)SQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
-            if (tgt && warp == 2)
+                bulk_g2s(dst + LY::sq_off_bytes(i), plane + (size_t)SQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
+            if (tgt) {
                 bulk_g2s(dst + LY::w_off, T.wxi2 + ((size_t)t*NY + P.y0)*128, (unsigned)(TY*128*sizeof(float)), bar);
-            if (tgt && warp == 3) bulk_g2s(dst + LY::f0_off, fo + ((size_t)t*NY + P.y0)*NX, TY*row_bytes, bar);
+                bulk_g2s(dst + LY::f0_off, fo + ((size_t)t*NY + P.y0)*NX, TY*row_bytes, bar);
+            }
         }
     }
 

@@ -36,7 +36,7 @@ import re
 import subprocess
 import sys
 
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("ISLBM_REFERENCE_ROOT", "/root/reference")
 CODE_DIR = os.path.join(REF_ROOT, "筆記：金的code", "0.可更改的code")
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")

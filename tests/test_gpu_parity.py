@@ -213,6 +213,50 @@ def test_tiled_wide_grid_vs_oracle(islbm_lib, oracle_mod, nx):
 
 
 
+@pytest.mark.slow
+@pytest.mark.parametrize("prec,tol_rho,tol_u", [("fp32", 1e-4, 5e-4), ("fp16", 1e-3, 2e-2)])
+def test_tiled_hill64_1000_steps_vs_oracle(islbm_lib, oracle_mod, prec, tol_rho, tol_u):
+    """The tiled kernel over the FP64 parity case's horizon: 64x32x48, 1000 steps, controller on,
+    tau = 0.6, against the FP64 oracle (FP32 arithmetic; FP16 also stores deviations in FP16)."""
+    steps = 1000
+    re = re_for_tau(0.6, 48)
+    g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision=prec, Re=re, kernel=2)
+    r = oracle_run(oracle_mod, steps, 32, 64, 48, ndtfrc=100, re=re)
+    e_rho, e_u = rel_l2(g["rho"], r["rho"]), rel_l2(velocity(g), velocity(r))
+    print(prec, "1000 steps: rho", e_rho, "u", e_u, "force", abs(g["force"] - r["force"]) / abs(r["force"]))
+    assert e_rho <= tol_rho
+    assert e_u <= tol_u
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp16", 2e-3)])
+@pytest.mark.parametrize("nx", [32, 64, 128, 256])
+def test_paired_matches_single_node_kernel(islbm_lib, prec, tol, nx):
+    """The paired-node tiled kernel against the one-node-per-thread tiled kernel (same storage,
+    FP32 arithmetic in a different order) on every width both compile, with LES and mass
+    correction on."""
+    steps = 30
+    re = re_for_tau(0.6 if nx <= 64 else 0.9, 48)
+    kw = dict(NX=nx, NY=32, NZ=48, NDTFRC=10, precision=prec, Re=re, les_cs=0.1, mass_interval=7)
+    a = solve(islbm_lib, steps, kernel=3, **kw)
+    b = solve(islbm_lib, steps, kernel=2, **kw)
+    assert rel_l2(b["rho"], a["rho"]) <= tol
+    assert rel_l2(velocity(b), velocity(a)) <= 50 * tol
+    assert abs(b["force"] - a["force"]) <= 1e-3 * abs(a["force"])
+
+
+@pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp16", 2e-3)])
+def test_tiled_384_tall_grid_vs_gather(islbm_lib, prec, tol):
+    """The 384-wide layout of the large benchmark grid on a tall column (NZ = 192, the benchmark
+    grid's wall-normal resolution) against the gather kernel."""
+    steps = 20
+    re = re_for_tau(1.0, 192)
+    kw = dict(NX=384, NY=16, NZ=192, NDTFRC=10, precision=prec, Re=re, les_cs=0.1, mass_interval=7)
+    a = solve(islbm_lib, steps, kernel=1, **kw)
+    b = solve(islbm_lib, steps, kernel=2, **kw)
+    assert rel_l2(b["rho"], a["rho"]) <= tol
+    assert rel_l2(velocity(b), velocity(a)) <= 50 * tol
+
+
 @pytest.mark.parametrize("prec", ["fp32", "fp16"])
 def test_spanwise_translation_invariance_full_size(islbm_lib, prec):
     """A size-independent property on the full 256x128x192 benchmark grid: the spanwise

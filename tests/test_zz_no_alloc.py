@@ -35,3 +35,20 @@ def test_noalloc_matches_allocating_entry_point(islbm_lib, precision):
                 for got, ref in ((got1, ref1), (got2, ref2)):
                     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=0)
                 assert np.all(np.isfinite(got1)) and abs(got1[0] - nx * ny * nz) < 1e-2 * nx * ny * nz
+
+
+def test_noalloc_refuses_grids_above_its_scratch(islbm_lib):
+    """A grid one plane above the fixed scratch's 33,554,432-node limit (384 x 288 x 304 =
+    33,619,968 nodes, FP16 storage, 2.6 GB) is refused with a message naming the limit, while the
+    allocating entry point serves it; nothing is launched for the refused call."""
+    islbm = islbm_lib
+    L = islbm.load()
+    p = islbm.default_params(NX=384, NY=288, NZ=304, Re=60.0, Uref=0.05, precision="fp16", init_mode=0)
+    with islbm.Solver(p) as s:
+        out = (ctypes.c_double * 4)()
+        st = L.islbm_diagnostics_noalloc(s._h, out)
+        assert st == 6   # ISLBM_ERR_NOT_SUPPORTED
+        msg = L.islbm_status_string(st).decode()
+        assert "33554432" in msg and "islbm_diagnostics" in msg, msg
+        ref = diag(L, "islbm_diagnostics", s._h)
+        assert abs(ref[0] - 384 * 288 * 304) < 1e-6 * 384 * 288 * 304
