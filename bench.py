@@ -35,8 +35,8 @@ for _p in (ROOT, PKG):
 
 METRIC = "ISLBM MLUPS & %HBM peak, mixed vs plain FP32 at stated err; serve p50/p99"
 # DRAM bytes of one launch of the FP32 step on this workload, from an ncu capture of the same
-# kernel (dram__bytes_read.sum + dram__bytes_write.sum: 521.7 MB + 440.4 MB)
-NCU_TRAFFIC_BYTES = 962.1e6
+# kernel (dram__bytes_read.sum + dram__bytes_write.sum: 590.3 MB + 433.0 MB)
+NCU_TRAFFIC_BYTES = 1023.3e6
 CASE = dict(NX=128, NY=256, NZ=192, Re=2800.0, Uref=0.05, NDTFRC=100, les_cs=0.1)
 WORKLOAD = "periodic hill 256x128x192 (streamwise x spanwise x wall-normal), Re_h 2800, LES Cs 0.1, Ub 0.05"
 
@@ -235,11 +235,10 @@ def large_accuracy_run(islbm, device, coarse_steps=300, samples=10):
            "samples": samples, "stations_x_over_h": [0.5, 2, 4, 6, 8], "coarse_healthy": ok_ref}
     for prec in ("fp32", "fp16"):
         prof, zf, ok, tf = profiles(fine, prec, every_f)
-        err = 0.0
-        for c in range(3):
-            for i in range(len(stations)):
-                err = max(err, float(np.max(np.abs(np.interp(zref[i], zf[i], prof[c, i]) - ref[c, i]))))
-        out[prec] = {"time_avg_profiles_max_abs_err_over_ub": err / fine["Uref"], "healthy": ok, "seconds": tf}
+        dev = [np.abs(np.interp(zref[i], zf[i], prof[c, i]) - ref[c, i]) for c in range(3) for i in range(len(stations))]
+        err = float(np.max(dev)) / fine["Uref"]
+        out[prec] = {"time_avg_profiles_max_abs_err_over_ub": err if ok and ok_ref and np.isfinite(err) else None,
+                     "healthy": ok, "seconds": tf}
     return out
 
 
@@ -325,30 +324,54 @@ def accuracy_run(islbm, device, steps=1000):
             "errors": out}
 
 
-def serve_run(islbm, nreq, device):
-    """Request stream through the serving loop and as sequential plain solves."""
+def serve_run(islbm, nreq, device, mean_gap=0.5, n_err=8):
+    """The specified request stream (Poisson arrivals) through the serving loop and as sequential
+    plain solves, with per-grid accounting; then the error against plain FP64 solves for n_err
+    requests of the stream (the two smaller grids; the FP64 step runs at a fraction of a GLUPS),
+    each served in one batch for 1000 steps and solved alone in FP64 for the same steps."""
     import numpy as np
     import serving
-    reqs = serving.make_requests(nreq, seed=2024, mean_gap=0.05)
-    small = [i for i, r in enumerate(reqs) if r["NZ"] == 48][:2]
-    srv, infos, fields = serving.run_server(reqs, steps_per_chunk=500, device=device, keep=small)
-    seq = serving.run_sequential(reqs, steps_per_check=500, device=device)
+    reqs = serving.make_requests(nreq, seed=2024, mean_gap=mean_gap)
+    srv, infos, _ = serving.run_server(reqs, device=device)
+    seq = serving.run_sequential(reqs, device=device)
+    grids = {}
+    for i, r in enumerate(reqs):
+        g = grids.setdefault("%dx%dx%d" % (r["NY"], r["NX"], r["NZ"]), {"requests": 0, "updates": 0, "converged": 0,
+                                                                         "steps": []})
+        g["requests"] += 1
+        g["updates"] += infos[i]["steps"] * r["NX"] * r["NY"] * r["NZ"]
+        g["converged"] += infos[i]["status"] == "converged"
+        g["steps"].append(infos[i]["steps"])
+    total = sum(g["updates"] for g in grids.values())
+    for g in grids.values():
+        g["share_of_updates"] = g["updates"] / max(total, 1)
+        st = g.pop("steps")
+        g["steps_median"] = float(np.median(st))
+    sample = [i for i, r in enumerate(reqs) if r["NZ"] == 48][:n_err // 2] + \
+             [i for i, r in enumerate(reqs) if r["NZ"] == 96][:n_err - n_err // 2]
     errs = []
-    for i in small:
+    steps = 1000
+    with islbm.Server(device=device, steps_per_chunk=steps) as s_err:
+        ids = {i: s_err.submit(serving.params_of(reqs[i]), steps, 0.0, keep_fields=True) for i in sample}
+        s_err.drain()
+        got = {i: s_err.fields(ids[i]) for i in sample}
+    for i in sample:
         r = reqs[i]
         with islbm.Solver(serving.params_of(r, precision="fp64", device=device)) as s:
-            s.step(infos[i]["steps"])
+            s.step(steps)
             ref = s.fields()
-        g = fields[i]
-        errs.append({"request": i, "precision": r["precision"], "steps": infos[i]["steps"],
+        g = got[i]
+        errs.append({"request": i, "grid": "%dx%dx%d" % (r["NY"], r["NX"], r["NZ"]), "precision": r["precision"],
+                     "alpha": r["alpha"], "steps": steps,
                      "rel_l2_u_vs_fp64": rel_l2(np.stack([g[c] for c in "uvw"]), np.stack([ref[c] for c in "uvw"])),
                      "max_abs_u_over_ub": float(max(np.abs(g[c] - ref[c]).max() for c in "uvw") / r["Uref"])})
-    return {"requests": nreq, "mean_gap_s": 0.05, "grids": "64x32x48 / 128x64x96 / 256x128x192 (NY x NX x NZ)",
+    return {"requests": nreq, "mean_gap_s": mean_gap, "grids": "64x32x48 / 128x64x96 / 256x128x192 (NY x NX x NZ)",
             "steps_cap": {"x".join(map(str, g)): c for g, c, _ in serving.GRIDS},
-            "tau_range": {"x".join(map(str, g)): list(t) for g, _, t in serving.GRIDS}, "alphas": list(serving.ALPHAS),
-            "tol": reqs[0]["tol"], "chunk": 500,
+            "tau_range": {"x".join(map(str, g)): list(t) for g, _, t in serving.GRIDS},
+            "alpha_range": list(serving.ALPHA_RANGE), "tol": serving.TOL, "chunk": serving.CHUNK,
+            "convergence": "delta = sqrt(mean |u - u_prev|^2)/Ub over each chunk < tol",
             "server": srv, "sequential": seq, "speedup_mlups": srv["mlups"] / seq["mlups"],
-            "error_vs_fp64": errs}
+            "per_grid": grids, "error_vs_fp64": errs}
 
 
 def slowest_rank_ms(ms, world, device):
@@ -379,7 +402,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-large", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=16)
+    ap.add_argument("--serve-requests", type=int, default=64)
     args = ap.parse_args()
     rank, world, local = dist_env()
     threads = os.cpu_count() or 1

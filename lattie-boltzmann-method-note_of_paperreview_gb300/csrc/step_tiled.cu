@@ -276,17 +276,20 @@ struct TiledKernel {
     }
 
     // Thread 0, at the end of the kernel: bounded wait for copies still pending (only after a
-    // timeout; in a healthy run every copy has been consumed).
+    // timeout; in a healthy run every copy has been consumed). A wait that runs out here is
+    // recorded as a fault too (bit 2), so the host learns of it even when no earlier wait failed.
     __device__ __forceinline__ void drain(unsigned char *smem, unsigned parity, int tid) const {
         if (tid != 0) return;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         for (int s = 0; s < LY::NS; s++) {
             if (!((parity >> (PEND + s)) & 1u)) continue;
             const unsigned ph = (parity >> (PPAR + s)) & 1u;
-            for (int it = 0; it < (1 << 22); ++it) {
-                if (mbar_try_wait(&bars[s], ph)) break;
-                if (it > 32) __nanosleep(256);
+            bool done = false;
+            for (int it = 0; it < (1 << 22) && !done; ++it) {
+                done = mbar_try_wait(&bars[s], ph);
+                if (!done && it > 32) __nanosleep(256);
             }
+            if (!done) atomicOr(&ctrl->fault, 2u);
         }
     }
 

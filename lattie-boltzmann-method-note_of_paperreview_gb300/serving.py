@@ -7,8 +7,17 @@ spanwise x wall-normal), the relaxation time (hence Re_h on that grid), the hill
 alpha and the storage format. Relaxation times are drawn from a range in which the reference
 step is stable on that grid: [0.6, 0.68] on 64x32x48, [0.9, 1.0] on 128x64x96, [1.0, 1.1] on
 256x128x192 (the scheme needs a larger tau on finer grids; Re_h in the thousands, tau near 1/2,
-diverges on all three). The hill steepness is one of ALPHAS: the reference step also diverges
-for some hill shapes in between (alpha 0.9 at tau 0.6 and alpha 1.12 at tau 0.625 on 64x32x48).
+diverges on all three). The steepness is drawn uniformly from ALPHA_RANGE: the reference step
+diverges within a thousand steps for many hill shapes, in narrow bands scattered over
+[0.5, 1.5] (scans in steps of 0.05, then 0.01 near the stable values, over the three grids and
+their tau ranges); [0.71, 0.76] is the widest interval stable at every scanned point of every
+grid and tau of the stream.
+
+Convergence: a solve retires when delta = sqrt(mean |u - u_prev|^2)/U_b over CHUNK = 1000
+steps falls below TOL, or at its grid's step cap. From a seeded perturbed start the flow keeps
+a slow transient with controller-driven oscillations: delta falls to a few 1e-2 within
+10-20 thousand steps on the two smaller grids and stays above 1e-2 over 40 thousand steps, so
+TOL is 5e-2 (a tolerance of 1e-5 is not reached within any practical cap).
 """
 import time
 
@@ -17,15 +26,18 @@ import numpy as np
 import islbm
 
 # (streamwise NY, spanwise NX, wall-normal NZ), the step cap and the stable tau range of each grid
-GRIDS = [((64, 32, 48), 6000, (0.6, 0.68)), ((128, 64, 96), 3000, (0.9, 1.0)), ((256, 128, 192), 1500, (1.0, 1.1))]
-ALPHAS = (0.8, 1.0)
+GRIDS = [((64, 32, 48), 20000, (0.6, 0.68)), ((128, 64, 96), 16000, (0.9, 1.0)), ((256, 128, 192), 2000, (1.0, 1.1))]
+ALPHA_RANGE = (0.71, 0.76)
+CHUNK = 1000
+TOL = 5e-2
 
 
 def min_size(NZ, LZ=3.036, CFL=0.6):
     return (LZ - 1.0) / NZ * CFL
 
 
-def make_requests(n, seed=2024, mean_gap=0.05, precisions=("fp32", "fp16"), tol=1e-5, cap_scale=1.0):
+def make_requests(n, seed=2024, mean_gap=0.5, precisions=("fp32", "fp16"), tol=TOL, cap_scale=1.0,
+                  alpha_range=ALPHA_RANGE):
     """n requests with exponential inter-arrival gaps (mean `mean_gap` seconds)."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -34,7 +46,7 @@ def make_requests(n, seed=2024, mean_gap=0.05, precisions=("fp32", "fp16"), tol=
         t += rng.exponential(mean_gap)
         (ny, nx, nz), cap, (tlo, thi) = GRIDS[rng.integers(len(GRIDS))]
         tau = rng.uniform(tlo, thi)
-        alpha = ALPHAS[rng.integers(len(ALPHAS))]
+        alpha = float(rng.uniform(*alpha_range))
         prec = precisions[rng.integers(len(precisions))]
         ub = 0.05
         re = 3.0 * ub / ((tau - 0.5) * min_size(nz))
@@ -56,7 +68,7 @@ def _stats(lat):
             "mean_s": float(lat.mean()), "max_s": float(lat.max())}
 
 
-def run_server(reqs, steps_per_chunk=500, hbm_budget_bytes=150 << 30, device=0, keep=()):
+def run_server(reqs, steps_per_chunk=CHUNK, hbm_budget_bytes=150 << 30, device=0, keep=()):
     """Submit each request at its arrival time, pump until all retired. Returns a summary and the
     per-request info (fields of the request indices in `keep` are kept)."""
     with islbm.Server(device=device, hbm_budget_bytes=hbm_budget_bytes, steps_per_chunk=steps_per_chunk) as srv:
@@ -92,15 +104,17 @@ def run_server(reqs, steps_per_chunk=500, hbm_budget_bytes=150 << 30, device=0, 
         infos, fields
 
 
-def run_sequential(reqs, steps_per_check=500, device=0):
+def run_sequential(reqs, steps_per_check=CHUNK, device=0):
     """The same requests as plain solves, one at a time in arrival order (each starts at its arrival or
     when the previous one ends), with the same convergence check every `steps_per_check` steps."""
     t0 = time.monotonic()
     lat, updates = [], 0
+    per_grid = {}
     for r in reqs:
         now = time.monotonic() - t0
         if now < r["arrival"]:
             time.sleep(r["arrival"] - now)
+        t_start = time.monotonic()
         with islbm.Solver(params_of(r, device=device)) as s:
             n = r["NX"] * r["NY"] * r["NZ"]
             f = s.fields()   # initial state, as the server's first snapshot
@@ -118,8 +132,14 @@ def run_sequential(reqs, steps_per_check=500, device=0):
                     break
                 prev = u
             updates += steps * n
+        g = per_grid.setdefault("%dx%dx%d" % (r["NY"], r["NX"], r["NZ"]), {"requests": 0, "updates": 0, "seconds": 0.0})
+        g["requests"] += 1
+        g["updates"] += steps * n
+        g["seconds"] += time.monotonic() - t_start
         lat.append(time.monotonic() - t0 - r["arrival"])
     wall = time.monotonic() - t0
     first = min(r["arrival"] for r in reqs)
+    for g in per_grid.values():   # each grid's requests run alone: their own rate, set-up included
+        g["mlups_alone"] = g["updates"] / max(g["seconds"], 1e-9) / 1e6
     return {"updates": updates, "wall_s": wall, "mlups": updates / max(wall - first, 1e-9) / 1e6,
-            "latency": _stats(lat)}
+            "latency": _stats(lat), "per_grid": per_grid}

@@ -214,10 +214,12 @@ def test_tiled_wide_grid_vs_oracle(islbm_lib, oracle_mod, nx):
 
 
 @pytest.mark.slow
-@pytest.mark.parametrize("prec,tol_rho,tol_u", [("fp32", 1e-4, 5e-4), ("fp16", 1e-3, 2e-2)])
+@pytest.mark.parametrize("prec,tol_rho,tol_u", [("fp32", 8e-5, 2e-4), ("fp16", 4e-5, 7e-4)])
 def test_tiled_hill64_1000_steps_vs_oracle(islbm_lib, oracle_mod, prec, tol_rho, tol_u):
     """The tiled kernel over the FP64 parity case's horizon: 64x32x48, 1000 steps, controller on,
-    tau = 0.6, against the FP64 oracle (FP32 arithmetic; FP16 also stores deviations in FP16)."""
+    tau = 0.6, against the FP64 oracle (FP32 arithmetic; FP16 also stores deviations in FP16).
+    Measured on a GB300: FP32 rho 2.1e-5, u 4.3e-5; FP16 rho 8.7e-6, u 1.7e-4; the tolerances
+    are about four times these."""
     steps = 1000
     re = re_for_tau(0.6, 48)
     g = solve(islbm_lib, steps, NX=32, NY=64, NZ=48, NDTFRC=100, precision=prec, Re=re, kernel=2)

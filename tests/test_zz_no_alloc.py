@@ -51,4 +51,5 @@ def test_noalloc_refuses_grids_above_its_scratch(islbm_lib):
         msg = L.islbm_status_string(st).decode()
         assert "33554432" in msg and "islbm_diagnostics" in msg, msg
         ref = diag(L, "islbm_diagnostics", s._h)
-        assert abs(ref[0] - 384 * 288 * 304) < 1e-6 * 384 * 288 * 304
+        # the rest state held as FP16 deviations: the mass to FP16 rounding of the deviations
+        assert abs(ref[0] - 384 * 288 * 304) < 1e-4 * 384 * 288 * 304
