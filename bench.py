@@ -193,52 +193,36 @@ def large_run(islbm, torch, device, steps=10, warmup=3):
     return out
 
 
-def large_accuracy_run(islbm, device, coarse_steps=300, samples=10):
-    """Accuracy of the large grid (768x384x512) against an FP64 run of the benchmark grid
-    (256x128x192): time-averaged u, v, w profiles at x/h = 0.5, 2, 4, 6, 8, the fine profiles
-    interpolated (linearly in the wall-normal coordinate) to the coarse nodes of the same column.
-    Both grids run the same physical case: U_b = 0.04, LES C_s = 0.1, and one Reynolds number at
-    which the reference scheme is stable on both (tau = 1.0 on the coarse grid, hence tau = 1.83
-    on the fine one); the same physical time (dt = minSize, so 8/3 fine steps per coarse step)
-    and the same sampling instants. The error is dominated by the grids' discretisation
-    difference; FP32 and FP16 storage are compared with the same coarse reference."""
+def large_accuracy_run(islbm, device, steps=800, samples=10, tau=1.1):
+    """Storage-format accuracy of the large grid (768x384x512): time-averaged u, v, w profiles of
+    the FP16-deviation run against the FP32 run of the same case, at x/h = 0.5, 2, 4, 6, 8 (the
+    stations of C/fileIO.h:118-249). The case is the one relaxation time at which the reference
+    scheme holds on this grid (tau = 1.1; it diverges within a few hundred steps at 0.6-1.0 and
+    1.2-2.5). The comparison the configuration names, against an FP64 run of 256x128x192 at the
+    same Reynolds number, has no common stable case: the same viscosity puts the coarse grid at
+    tau = 0.725, where it grows without bound within 300 steps (the coarse grid holds only from
+    tau = 1.0 up, which puts the fine grid at 1.83)."""
     import numpy as np
-    coarse = dict(NX=128, NY=256, NZ=192, Uref=0.04, NDTFRC=100, les_cs=0.1)
-    fine = dict(NX=384, NY=768, NZ=512, Uref=0.04, NDTFRC=100, les_cs=0.1)
-    ms_c = (3.036 - 1.0) / coarse["NZ"] * 0.6
-    re = 3.0 * coarse["Uref"] / (0.5 * ms_c)
-    ratio = fine["NZ"] / coarse["NZ"]                       # 8/3 fine steps per coarse step
-    every_c = coarse_steps // samples
-    every_f = int(round(every_c * ratio))
-    assert abs(every_f - every_c * ratio) < 1e-9
-    stations = [int(round(st * coarse["NY"] / 9.0)) % coarse["NY"] for st in (0.5, 2.0, 4.0, 6.0, 8.0)]
-    scale = fine["NY"] // coarse["NY"]                       # coarse row y is fine row 3y (same position)
-
-    def profiles(case, prec, every):
+    case = dict(NX=384, NY=768, NZ=512, Uref=0.04, NDTFRC=100, les_cs=0.1)
+    ms_f = (3.036 - 1.0) / case["NZ"] * 0.6
+    re = 3.0 * case["Uref"] / ((tau - 0.5) * ms_f)
+    rows = [int(round(st * case["NY"] / 9.0)) % case["NY"] for st in (0.5, 2.0, 4.0, 6.0, 8.0)]
+    out = {"case": "768x384x512, %d steps, tau %.2f (Re_h %.1f), LES Cs 0.1, Ub 0.04" % (steps, tau, re),
+           "samples": samples, "stations_x_over_h": [0.5, 2, 4, 6, 8]}
+    prof = {}
+    for prec in ("fp32", "fp16"):
         p = islbm.default_params(precision=prec, device=device, Re=re, **case)
-        z = islbm.host_table(p, "z").reshape(case["NY"] + 7, case["NZ"] + 6)
-        rows = stations if case is coarse else [scale * y for y in stations]
         t0 = time.perf_counter()
         with islbm.Solver(p) as s:
             s.stats_reset()
             for _ in range(samples):
-                s.step(every)
+                s.step(steps // samples)
                 s.stats_accumulate()
-            prof = np.stack([[s.stats_profile(q, y) for y in rows] for q in ("U", "V", "W")])
-            healthy = s.healthy()
-        zc = np.stack([z[y + 3, 3:3 + case["NZ"]] for y in rows])
-        return prof, zc, healthy, time.perf_counter() - t0
-
-    ref, zref, ok_ref, _ = profiles(coarse, "fp64", every_c)
-    out = {"coarse": "256x128x192 FP64, %d steps, tau 1.0 (Re_h %.1f)" % (coarse_steps, re),
-           "fine": "768x384x512, %d steps, tau %.3f" % (every_f * samples, 0.5 + 0.5 * ratio),
-           "samples": samples, "stations_x_over_h": [0.5, 2, 4, 6, 8], "coarse_healthy": ok_ref}
-    for prec in ("fp32", "fp16"):
-        prof, zf, ok, tf = profiles(fine, prec, every_f)
-        dev = [np.abs(np.interp(zref[i], zf[i], prof[c, i]) - ref[c, i]) for c in range(3) for i in range(len(stations))]
-        err = float(np.max(dev)) / fine["Uref"]
-        out[prec] = {"time_avg_profiles_max_abs_err_over_ub": err if ok and ok_ref and np.isfinite(err) else None,
-                     "healthy": ok, "seconds": tf}
+            prof[prec] = np.stack([[s.stats_profile(q, y) for y in rows] for q in ("U", "V", "W")])
+            out[prec] = {"healthy": s.healthy(), "seconds": time.perf_counter() - t0,
+                         "max_abs_profile_over_ub": float(np.abs(prof[prec]).max() / case["Uref"])}
+    err = float(np.abs(prof["fp16"] - prof["fp32"]).max() / case["Uref"])
+    out["fp16"]["time_avg_profiles_max_abs_err_vs_fp32_over_ub"] = err if np.isfinite(err) else None
     return out
 
 
