@@ -318,6 +318,14 @@ def serve_run(islbm, nreq, device, mean_gap=0.5, n_err=8):
     reqs = serving.make_requests(nreq, seed=2024, mean_gap=mean_gap)
     srv, infos, _ = serving.run_server(reqs, device=device)
     seq = serving.run_sequential(reqs, device=device)
+    # capacity: the same requests all submitted at once, against the same plain solves back to
+    # back (their summed solve time, set-up included)
+    sat, _, _ = serving.run_server([dict(r, arrival=0.0) for r in reqs], device=device)
+    seq_busy = sum(g["seconds"] for g in seq["per_grid"].values())
+    capacity = {"server_mlups": sat["mlups"], "server_wall_s": sat["wall_s"], "server_updates": sat["updates"],
+                "sequential_mlups": seq["updates"] / max(seq_busy, 1e-9) / 1e6, "sequential_busy_s": seq_busy,
+                "speedup_mlups": sat["mlups"] / max(seq["updates"] / max(seq_busy, 1e-9) / 1e6, 1e-9),
+                "status": sat["status"]}
     grids = {}
     for i, r in enumerate(reqs):
         g = grids.setdefault("%dx%dx%d" % (r["NY"], r["NX"], r["NZ"]), {"requests": 0, "updates": 0, "converged": 0,
@@ -354,7 +362,7 @@ def serve_run(islbm, nreq, device, mean_gap=0.5, n_err=8):
             "tau_range": {"x".join(map(str, g)): list(t) for g, _, t in serving.GRIDS},
             "alpha_range": list(serving.ALPHA_RANGE), "tol": serving.TOL, "chunk": serving.CHUNK,
             "convergence": "delta = sqrt(mean |u - u_prev|^2)/Ub over each chunk < tol",
-            "server": srv, "sequential": seq, "speedup_mlups": srv["mlups"] / seq["mlups"],
+            "server": srv, "sequential": seq, "speedup_mlups": srv["mlups"] / seq["mlups"], "capacity": capacity,
             "per_grid": grids, "error_vs_fp64": errs}
 
 
