@@ -13,8 +13,12 @@
  *     retires solves that converged, diverged or reached their cap;
  *   - islbm_server_info / islbm_server_fields report a request's state, timings and result.
  *
- * Convergence: after each chunk, delta = sqrt(mean over nodes of |u - u_prev|^2) / Uref, with
- * u_prev the velocity at the previous check; a solve retires as converged when delta < tol.
+ * Convergence: every steps_per_chunk steps of a solve (counted from its admission),
+ * delta = sqrt(mean over nodes of |u - u_prev|^2) / Uref, with u_prev the velocity at the
+ * previous check (the initial state for the first); a solve retires as converged when
+ * delta < tol. A chunk ends at the next check or cap of any active solve, so a check always
+ * spans exactly steps_per_chunk steps; a solve that reaches its cap between checks retires as
+ * capped.
  * A request whose memory alone exceeds the budget is rejected. Results are identical to running
  * the same parameters alone through islbm_init/islbm_step: the batched launch applies the same
  * per-solve arithmetic and the same tile decomposition.

@@ -7,9 +7,11 @@
 //      format and spanwise width are stepped by one batched tiled launch per step, the chunk
 //      of launches captured once per batch composition in a CUDA graph and replayed; other
 //      solves use their own step kernel;
-//   3. measures the relative change of each solve's velocity field over the chunk on the
-//      device (one scalar per solve read back) and retires solves that converged, diverged
-//      or reached their step cap, freeing their memory for the queue.
+//   3. measures the relative change of the velocity field of each solve that has completed
+//      steps_per_chunk steps since its previous check (one scalar per solve read back) and
+//      retires solves that converged, diverged or reached their step cap, freeing their memory
+//      for the queue. A chunk ends at the next check or cap of any active solve, so every
+//      check of every solve spans exactly steps_per_chunk of its steps, whenever it arrived.
 // The launch shape of each batch (persistent CTAs per SM) is picked by a small autotuner that
 // times the candidates on the first steps of a new batch composition and caches the winner.
 #include <algorithm>
@@ -96,6 +98,7 @@ struct Solve {
     void *snap = nullptr;       // velocity at the previous convergence check (compute type)
     size_t bytes = 0;
     long long steps = 0;
+    long long since_check = 0;  // steps since the previous convergence check (or admission)
     double delta = -1.0;
     int status = ISLBM_SOLVE_QUEUED;
     double t_submit = 0, t_admit = 0, t_done = 0;
@@ -318,17 +321,20 @@ cudaError_t launch_batch(Group *g, int grid, int macros_on) {
 
 // Autotuner: candidate persistent-CTA counts for a batch, timed on one real step each.
 // Returns a status; the timed launches advance every member and are accounted for here.
-int tune(islbm_server *s, Group *g) {
+// Picks the group's CTA count. The timed candidate launches are real steps of every member:
+// at most `budget` of them, their number returned in `launched`.
+int tune(islbm_server *s, Group *g, int budget, int &launched) {
+    launched = 0;
     const std::string sig = std::to_string(g->precision) + "/" + std::to_string(g->NX) + "/" + std::to_string(g->les) +
                             "/" + std::to_string(g->nitems);
     auto it = s->tuned_grid.find(sig);
     if (it != s->tuned_grid.end()) { g->grid = it->second; return ISLBM_OK; }
-    // every member must have room for the tuning steps under its cap
-    for (Solve *v : g->members)
-        if (v->max_steps - v->steps < 3) { g->grid = std::min(g->nitems, 2*s->sms); return ISLBM_OK; }
     const int cand[3] = {std::min(g->nitems, s->sms), std::min(g->nitems, 2*s->sms), std::min(g->nitems, 4*s->sms)};
+    // the tuning steps must fit in this chunk (they count toward it); otherwise this batch
+    // composition keeps the default shape
+    if (budget < 3) { g->grid = cand[1]; return ISLBM_OK; }
     float best = 1e30f;
-    int best_grid = cand[0], launched = 0;
+    int best_grid = cand[0];
     cudaEvent_t e0, e1;
     SK(cudaEventCreate(&e0));
     SK(cudaEventCreate(&e1));
@@ -428,21 +434,23 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
         fresh.clear();
     }
     if (!s->active.empty()) {
-        // chunk length: up to the next convergence check / step cap of any active solve
+        // chunk length: up to the next convergence check or step cap of any active solve
         int steps = s->chunk;
-        for (Solve *v : s->active) steps = (int)std::min<long long>(steps, std::max<long long>(1, v->max_steps - v->steps));
+        for (Solve *v : s->active)
+            steps = (int)std::min<long long>(steps, std::max<long long>(1, std::min<long long>(s->chunk - v->since_check,
+                                                                                             v->max_steps - v->steps)));
         std::vector<Group *> groups;
         std::vector<Solve *> singles;
         st = build_groups(s, groups, singles);
         if (st != ISLBM_OK) return st;
         for (Group *g : groups) {
+            int tuned = 0;
             if (!g->grid) {
-                st = tune(s, g);
+                st = tune(s, g, steps, tuned);
                 if (st != ISLBM_OK) return st;
             }
             // the tuning steps count toward the chunk; what remains runs as one graph
-            int left = steps;
-            for (Solve *v : g->members) left = (int)std::min<long long>(left, v->max_steps - v->steps);
+            const int left = steps - tuned;
             if (left > 0) {
                 st = run_group_chunk(s, g, left);
                 if (st != ISLBM_OK) return st;
@@ -456,6 +464,7 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             v->steps += steps;
             s->updates += (long long)steps*(long long)v->h->N;
         }
+        for (Solve *v : s->active) v->since_check += steps;
         // the convergence measure (on the server stream) waits for every batch
         for (Group *g : groups) {
             SK(cudaEventRecord(g->done, g->stream));
@@ -476,7 +485,9 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             SK(cudaMalloc(&s->dsum, s->dsum_cap*sizeof(double)));
         }
         SK(cudaMemsetAsync(s->dsum, 0, s->active.size()*sizeof(double), s->stream));
-        for (size_t i = 0; i < s->active.size(); i++) SK(launch_delta(s->active[i]->h, s->active[i]->snap, s->dsum + i, s->stream));
+        // only solves at the end of a full check interval are measured (their snapshot advances)
+        for (size_t i = 0; i < s->active.size(); i++)
+            if (s->active[i]->since_check >= s->chunk) SK(launch_delta(s->active[i]->h, s->active[i]->snap, s->dsum + i, s->stream));
         std::vector<double> sums(s->active.size());
         SK(cudaMemcpyAsync(sums.data(), s->dsum, sums.size()*sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         SK(cudaStreamSynchronize(s->stream));
@@ -484,7 +495,11 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
         for (size_t i = 0; i < s->active.size(); i++) {
             Solve *v = s->active[i];
             const double n = (double)v->h->N;
-            v->delta = std::sqrt(sums[i]/n)/v->p.Uref;
+            const bool checked = v->since_check >= s->chunk;
+            if (checked) {
+                v->delta = std::sqrt(sums[i]/n)/v->p.Uref;
+                v->since_check = 0;
+            }
             // a timed-out pipeline wait in the step kernel leaves the state undefined
             st = islbm_sync(v->h);
             if (st != ISLBM_OK) { s->last = "step kernel pipeline wait timed out"; return st; }
@@ -493,7 +508,7 @@ int islbm_server_pump(islbm_server *s, int *n_active, int *n_queued) {
             // a change of the velocity by more than a thousand times the bulk velocity between two
             // checks only happens on the way to overflow
             if (fin != ISLBM_OK || !(v->delta <= 1e3)) retire(s, v, ISLBM_SOLVE_DIVERGED);
-            else if (v->delta < v->tol) retire(s, v, ISLBM_SOLVE_CONVERGED);
+            else if (checked && v->delta < v->tol) retire(s, v, ISLBM_SOLVE_CONVERGED);
             else if (v->steps >= v->max_steps) retire(s, v, ISLBM_SOLVE_CAPPED);
             else keep.push_back(v);
         }

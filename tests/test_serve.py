@@ -134,3 +134,24 @@ def test_continuous_batching_admits_mid_flight(islbm_lib):
             err_rho, err_u = rel_l2(got["rho"], ref["rho"]), rel_l2(vel(got), vel(ref))
             assert err_rho <= TOL[prec] and err_u <= 10 * TOL[prec], (k, err_rho, err_u)
             assert abs(info["force"] - force) <= 1e-6 * abs(force) + 1e-12, k
+
+
+def test_checks_span_full_chunks(islbm_lib):
+    """Every convergence check of a solve spans exactly steps_per_chunk of its own steps: the
+    autotuner's timed steps count toward the chunk, a solve that arrives while another is at
+    its cap still gets a full first interval, and a solve whose cap comes before its first full
+    interval retires as capped even with a tolerance it would meet on a shorter interval."""
+    islbm = islbm_lib
+    chunk = 50
+    p = stable(islbm, precision="fp32")
+    with islbm.Server(steps_per_chunk=chunk) as srv:
+        a = srv.submit(p, max_steps=120, tol=0.0)            # tuned on its first chunk
+        srv.pump()
+        assert srv.info(a)["steps"] == chunk
+        b = srv.submit(p, max_steps=10_000, tol=10.0)        # new composition: tuned again
+        c = srv.submit(p, max_steps=30, tol=10.0)            # capped before any check
+        srv.drain()
+        ia, ib, ic = srv.info(a), srv.info(b), srv.info(c)
+        assert ia["status"] == "capped" and ia["steps"] == 120
+        assert ib["status"] == "converged" and ib["steps"] == chunk, ib
+        assert ic["status"] == "capped" and ic["steps"] == 30 and ic["delta"] == -1.0, ic
