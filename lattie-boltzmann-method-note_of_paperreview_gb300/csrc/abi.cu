@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <new>
@@ -444,6 +445,9 @@ int init_impl(const islbm_params *pp, islbm_handle *h) {
         if (p.kernel != ISLBM_KERNEL_TILED_SINGLE && pair_supported(k, p.precision) &&
             make_pair_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) == 0) {
             h->use_tiled = h->paired = true;
+            // tensor-map plane copies unless the bulk row copies are asked for (comparison runs)
+            const char *cp = std::getenv("ISLBM_PAIR_COPIES");
+            if (!(cp && std::strcmp(cp, "bulk") == 0)) make_pair_maps(k, (int)h->elem, h->fbuf, &h->pmaps);
         } else if (tiled_supported(k, p.precision) && make_tiled_const(k, p.precision, wx0, wx2, wy0, wy2, sms, &h->tiled) == 0) {
             h->use_tiled = true;
         }
@@ -520,6 +524,7 @@ int islbm_step(islbm_handle *h, int nsteps) {
         const unsigned long long n = h->steps + 1;
         L.fo = h->fbuf[h->cur];
         L.fn = h->fbuf[1 - h->cur];
+        L.pmaps = h->paired ? h->pmaps.for_buffer(L.fo) : nullptr;
         L.n = n;
         L.mass = h->p.mass_interval > 0 && (n % (unsigned long long)h->p.mass_interval) == 0ULL;
         L.macros_on = (s == nsteps - 1);

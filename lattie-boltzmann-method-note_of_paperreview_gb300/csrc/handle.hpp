@@ -38,6 +38,7 @@ struct islbm_handle {
 
     double *xfer = nullptr;    // FP64 transfer buffer of N values for host copies (first use)
     TiledConst tiled{};
+    PairMaps pmaps{};          // tensor maps of fbuf[0], fbuf[1] for the paired kernel's copies
 };
 
 

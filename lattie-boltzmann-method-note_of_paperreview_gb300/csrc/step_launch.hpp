@@ -19,6 +19,7 @@ struct StepLaunch {
     bool les, macros_on, mass;
     void *macros[4];           // rho, u, v, w (compute type) when macros_on
     const void *tiled;         // TiledConst for the tiled kernel
+    const void *pmaps;         // paired kernel: the 4 tensor maps (CUtensorMap) of buffer fo, or null
     cudaStream_t stream;
 };
 

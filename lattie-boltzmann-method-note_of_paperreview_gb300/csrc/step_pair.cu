@@ -7,9 +7,11 @@
 //     x0 = 2*(thread % (NX/2)) and x0 + 1) and marches upward through a wall-normal segment of
 //     that column; each plane's 18 moving populations are copied global -> shared memory by
 //     cp.async.bulk (the ten with e_y != 0 with a 3-row streamwise halo on both sides, periodic
-//     wrap by splitting the copy), issued by one thread: every operand is uniform over the CTA,
-//     so a copy costs a few uniform instructions (spreading the copies over four warps was
-//     slower: every issuing warp then stalls right after the barrier);
+//     wrap by splitting the copy); every operand of a copy is uniform over the CTA, so one
+//     thread issues it with a few uniform instructions. An issuing thread stalls for about 50
+//     cycles per copy, so the front copies are issued by thread 0 and the stage copies by
+//     thread 64 (another warp, of the other tile row where a tile has two): the two stalls
+//     overlap (4% faster than one issuer; splitting the front copies as well was slower);
 //   * front buffer (populations read before the plane's CTA barrier: the streamwise-filtered
 //     ten and the xi-only 5, 6) and stage buffer (1, 2, 11..14, read after it, plus the target
 //     row's xi weights and f0) have mbarriers of their own, so the front copies of plane p + 2
@@ -30,6 +32,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
+
+#include <cudaTypedefs.h>
 
 #include "pair_math.cuh"
 #include "step_common.cuh"
@@ -175,6 +179,20 @@ template <class S> __device__ __forceinline__ void st2(S *p, V2 v, int q) {
     }
 }
 
+// Tensor copy of one box (x, y, z, q) of a population buffer: the box lands in shared memory as
+// [q][rows][NX], the layout of the front and stage buffers.
+__device__ __forceinline__ void tma_load4(void *dst, const CUtensorMap *map, int x, int y, int z, int q, uint64_t *bar) {
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+                 ::"r"(smem_u32(dst)), "l"((unsigned long long)map), "r"(x), "r"(y), "r"(z), "r"(q), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// The four tensor maps of the buffer a launch reads (kernel parameter: tensor maps must live in
+// parameter, constant or global memory)
+struct PairTM {
+    CUtensorMap m[4];
+};
+
 template <int NX> __device__ __forceinline__ int pwrap(int v) {
     if constexpr ((NX & (NX - 1)) == 0) return v & (NX - 1);
     else return v < 0 ? v + NX : (v >= NX ? v - NX : v);
@@ -201,8 +219,8 @@ struct PairKernel {
     struct Piece {
         int y0, ta, tb, p0, p1;
     };
-    // pipeline word (every thread): bits 0..1 front parities, 2..3 stage parities; thread 0
-    // also keeps bits 8.. (pending copies of front f / stage s) and 16.. (their parities)
+    // pipeline word (every thread): bits 0..1 front parities, 2..3 stage parities; the issuing
+    // threads also keep bits 8.. (pending copies of front f / stage s) and 16.. (their parities)
     static constexpr int FP = 0, SP = 2, PENDF = 8, PENDS = 10, PPARF = 16, PPARS = 18;
 
     // Walls, BFL rows, collision and stores of the node pair (x0, x0 + 1) at row y, plane z,
@@ -257,12 +275,19 @@ struct PairKernel {
 
     // Copies of plane p: the front part into front buffer f and/or the stage part (with the target
     // rows of plane p - 3 when that target is staged) into stage s. Called by every thread after a
-    // CTA barrier; thread 0 issues every copy (its operands are uniform over the CTA), posting the
-    // expected bytes first and keeping the pending record for the drain.
+    // CTA barrier; thread FRONT_ISSUER issues the front copies and STAGE_ISSUER the stage copies
+    // (their operands are uniform over the CTA), each posting its buffer's expected bytes first and
+    // keeping the buffer's pending record for the drain.
+    static constexpr int FRONT_ISSUER = 0, STAGE_ISSUER = 64;
+    // tm: the buffer's tensor maps (box 0: 3, 4 and box 1: 7..10 / 15..18 over the TY + 6 rows;
+    // box 2: 5, 6 / 1, 2 and box 3: 11..14 over the TY rows), one copy per box; tiles whose halo
+    // wraps around the streamwise period, and launches without maps, copy row runs instead.
     __device__ __forceinline__ void issue(unsigned char *smem, int p, int f, int s, bool do_front, bool do_stage,
-                                          const Piece &P, unsigned &pipe, int tid) const {
+                                          const Piece &P, unsigned &pipe, int tid, const CUtensorMap *tm) const {
         constexpr int NX = LY::NX, TY = LY::TY;
-        if (tid != 0) return;
+        do_front = do_front && tid == FRONT_ISSUER;
+        do_stage = do_stage && tid == STAGE_ISSUER;
+        if (!do_front && !do_stage) return;
         if (*(volatile int *)(smem + LY::flag_off)) return;   // a wait timed out: no further copies
         if (p == k.drill_plane) return;                        // failure drill: this plane never arrives
         const int NY = k.NY;
@@ -276,19 +301,26 @@ struct PairKernel {
             mbar_expect_tx(bar, LY::front_tx());
             pipe = (pipe & ~(1u << (PPARF + f))) | (((pipe >> (FP + f)) & 1u) << (PPARF + f)) | (1u << (PENDF + f));
             unsigned char *dst = smem + LY::front_off(f);
-            const int ys = P.y0 >= 3 ? P.y0 - 3 : P.y0 - 3 + NY;
             constexpr int rows = TY + 6;
-            const int first = min(rows, NY - ys);
+            if (tm && P.y0 >= 3 && P.y0 + TY + 3 <= NY) {
+                tma_load4(dst + LY::fq_off_bytes(0), tm + 0, 0, P.y0 - 3, p, 3, bar);
+                tma_load4(dst + LY::fq_off_bytes(2), tm + 1, 0, P.y0 - 3, p, 7, bar);
+                tma_load4(dst + LY::fq_off_bytes(6), tm + 1, 0, P.y0 - 3, p, 15, bar);
+                tma_load4(dst + LY::fq_off_bytes(10), tm + 2, 0, P.y0, p, 5, bar);
+            } else {
+                const int ys = P.y0 >= 3 ? P.y0 - 3 : P.y0 - 3 + NY;
+                const int first = min(rows, NY - ys);
 #pragma unroll
-            for (int i = 0; i < 10; i++) {
-                S *d = (S *)(dst + LY::fq_off_bytes(i));
-                const S *src = plane + (size_t)FQ(i)*N;
-                bulk_g2s(d, src + (size_t)ys*NX, first*row_bytes, bar);
-                if (first < rows) bulk_g2s(d + (size_t)first*NX, src, (rows - first)*row_bytes, bar);
+                for (int i = 0; i < 10; i++) {
+                    S *d = (S *)(dst + LY::fq_off_bytes(i));
+                    const S *src = plane + (size_t)FQ(i)*N;
+                    bulk_g2s(d, src + (size_t)ys*NX, first*row_bytes, bar);
+                    if (first < rows) bulk_g2s(d + (size_t)first*NX, src, (rows - first)*row_bytes, bar);
+                }
+#pragma unroll
+                for (int i = 10; i < 12; i++)
+                    bulk_g2s(dst + LY::fq_off_bytes(i), plane + (size_t)FQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
             }
-#pragma unroll
-            for (int i = 10; i < 12; i++)
-                bulk_g2s(dst + LY::fq_off_bytes(i), plane + (size_t)FQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
         }
         if (do_stage) {
             uint64_t *bar = bars + LY::NF + s;
@@ -297,9 +329,14 @@ struct PairKernel {
             mbar_expect_tx(bar, LY::stage_tx + (tgt ? LY::tgt_tx : 0u));
             pipe = (pipe & ~(1u << (PPARS + s))) | (((pipe >> (SP + s)) & 1u) << (PPARS + s)) | (1u << (PENDS + s));
             unsigned char *dst = smem + LY::stage_off(s);
+            if (tm) {
+                tma_load4(dst + LY::sq_off_bytes(0), tm + 2, 0, P.y0, p, 1, bar);
+                tma_load4(dst + LY::sq_off_bytes(2), tm + 3, 0, P.y0, p, 11, bar);
+            } else {
 #pragma unroll
-            for (int i = 0; i < 6; i++)
-                bulk_g2s(dst + LY::sq_off_bytes(i), plane + (size_t)SQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
+                for (int i = 0; i < 6; i++)
+                    bulk_g2s(dst + LY::sq_off_bytes(i), plane + (size_t)SQ(i)*N + (size_t)P.y0*NX, TY*row_bytes, bar);
+            }
             if (tgt) {
                 bulk_g2s(dst + LY::w_off, T.wxi2 + ((size_t)t*NY + P.y0)*128, (unsigned)(TY*128*sizeof(float)), bar);
                 bulk_g2s(dst + LY::f0_off, fo + ((size_t)t*NY + P.y0)*NX, TY*row_bytes, bar);
@@ -307,14 +344,15 @@ struct PairKernel {
         }
     }
 
-    // Thread 0, at the end of the kernel: bounded wait for copies still pending (only after a
-    // timeout; in a healthy run every copy has been consumed). A wait that runs out here is
-    // recorded as a fault too.
+    // The issuing threads, at the end of the kernel: bounded wait for the copies they issued that
+    // are still pending (only after a timeout; in a healthy run every copy has been consumed). A
+    // wait that runs out here is recorded as a fault too.
     __device__ __forceinline__ void drain(unsigned char *smem, unsigned pipe, int tid) const {
-        if (tid != 0) return;
+        if (tid != FRONT_ISSUER && tid != STAGE_ISSUER) return;
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         for (int b = 0; b < LY::NF + LY::NS; b++) {
             const bool front = b < LY::NF;
+            if (tid != (front ? FRONT_ISSUER : STAGE_ISSUER)) continue;
             const int i = front ? b : b - LY::NF;
             if (!((pipe >> ((front ? PENDF : PENDS) + i)) & 1u)) continue;
             const unsigned ph = (pipe >> ((front ? PPARF : PPARS) + i)) & 1u;
@@ -341,7 +379,7 @@ struct PairKernel {
                                              int pend_bit, int tid) const {
         uint64_t *bars = (uint64_t *)(smem + LY::bar_off);
         if (mbar_wait(&bars[b], (pipe >> pbit) & 1u, ctrl, faulted)) {
-            if (tid == 0) pipe &= ~(1u << pend_bit);
+            pipe &= ~(1u << pend_bit);   // (meaningful in the issuer's word only)
         } else if (faulted) {
             *(volatile int *)(smem + LY::flag_off) = 1;
         }
@@ -350,7 +388,7 @@ struct PairKernel {
 
     // One source plane (the i-th of its piece): filter, store the plane's values in ring slot sp.
     __device__ __forceinline__ void plane(int i, int p, const Piece &P, unsigned char *smem, unsigned &pipe,
-                                          bool &faulted, const Lane &L, int sp) const {
+                                          bool &faulted, const Lane &L, int sp, const CUtensorMap *tm) const {
         constexpr int NX = LY::NX;
         const int f = LY::NF == 2 ? (i & 1) : 0, s = i & 1;
         wait_bar(smem, f, FP + f, pipe, faulted, PENDF + f, L.tid);
@@ -378,10 +416,10 @@ struct PairKernel {
         __syncthreads();
         // every thread has filtered plane p (front f free) and finished plane p-1 (stage s^1 free)
         if (LY::NF == 2) {
-            if (p + 2 <= P.p1) issue(smem, p + 2, f, 0, true, false, P, pipe, L.tid);
-            if (p + 1 <= P.p1) issue(smem, p + 1, 0, s ^ 1, false, true, P, pipe, L.tid);
+            if (p + 2 <= P.p1) issue(smem, p + 2, f, 0, true, false, P, pipe, L.tid, tm);
+            if (p + 1 <= P.p1) issue(smem, p + 1, 0, s ^ 1, false, true, P, pipe, L.tid, tm);
         } else if (p + 1 <= P.p1) {
-            issue(smem, p + 1, 0, s ^ 1, true, true, P, pipe, L.tid);
+            issue(smem, p + 1, 0, s ^ 1, true, true, P, pipe, L.tid, tm);
         }
         wait_bar(smem, LY::NF + s, SP + s, pipe, faulted, PENDS + s, L.tid);
         {   // spanwise filters
@@ -530,17 +568,17 @@ struct PairKernel {
     }
 
     __device__ __forceinline__ void piece(const Piece &P, unsigned char *smem, unsigned &pipe, bool &faulted,
-                                          const Lane &L, const Scal &sc, float &ub, V2 &mass) const {
+                                          const Lane &L, const Scal &sc, float &ub, V2 &mass, const CUtensorMap *tm) const {
         const int NZ = k.NZ;
         __syncthreads();   // every thread is done with every buffer of the previous piece
-        issue(smem, P.p0, 0, 0, true, true, P, pipe, L.tid);
-        if (LY::NF == 2 && P.p0 + 1 <= P.p1) issue(smem, P.p0 + 1, 1, 0, true, false, P, pipe, L.tid);
+        issue(smem, P.p0, 0, 0, true, true, P, pipe, L.tid, tm);
+        if (LY::NF == 2 && P.p0 + 1 <= P.p1) issue(smem, P.p0 + 1, 1, 0, true, false, P, pipe, L.tid, tm);
         const int y = P.y0 + L.yl;
         int sp = P.p0 % 7;
 #pragma unroll 1
         for (int p = P.p0; p <= P.p1; p++, sp = sp == 6 ? 0 : sp + 1) {
             const int i = p - P.p0;
-            plane(i, p, P, smem, pipe, faulted, L, sp);
+            plane(i, p, P, smem, pipe, faulted, L, sp, tm);
             if (i < 6) {
                 // the ring slots a target reads first must be complete: the newest plane's are
                 // waited for inside xi_combine, every older one by then
@@ -592,8 +630,9 @@ struct PairKernel {
         }
     }
 
-    __device__ void run() const {
+    __device__ void run(const CUtensorMap *tm) const {
         extern __shared__ __align__(128) unsigned char smem[];
+        if (smem_u32(smem) & 127u) tm = nullptr;   // tensor copies need 128-byte aligned destinations
         init_bars(smem, threadIdx.x);
         const Lane L = lane(ring_alloc(smem, threadIdx.x));   // ring_alloc includes the CTA barrier after the init
         unsigned pipe = 0;
@@ -612,7 +651,7 @@ struct PairKernel {
             P.p1 = window_base(P.tb - 1) + 6;
             float ub = 0.f;
             V2 mass = V2(0.f);
-            piece(P, smem, pipe, faulted, L, sc, ub, mass);
+            piece(P, smem, pipe, faulted, L, sc, ub, mass, tm);
             const float m = mass.v.x + mass.v.y;
             if (!isfinite(m)) ctrl->nonfinite = 1u;
             ub_total += (double)ub;
@@ -626,15 +665,19 @@ struct PairKernel {
 
 template <class S, bool LES, int NXC>
 struct PairBatchDesc {
+    CUtensorMap tm[2][4];   // tensor maps of buf[0], buf[1] (used when tm_on)
     PairKernel<S, LES, NXC> K;
     S *buf[2];          // population buffers; the old one is buf[step & 1]
     int ntiles;
     int nseg;
+    int tm_on;
 };
 
 template <class S, bool LES, int NXC>
 __global__ void __launch_bounds__(pair_threads<NXC>(), 512/PLay<S, NXC>::RING)
-step_pair_kernel(PairKernel<S, LES, NXC> K) { K.run(); }
+step_pair_kernel(const __grid_constant__ PairKernel<S, LES, NXC> K, const __grid_constant__ PairTM T, int tm_on) {
+    K.run(tm_on ? T.m : nullptr);
+}
 
 // Batched form (serving): work items (solve, segment*ntiles + tile) of many solves of the same
 // storage format and width; each CTA copies the item's solve descriptor into shared memory and
@@ -687,7 +730,8 @@ step_pair_batch_kernel(const PairBatchDesc<S, LES, NXC> *__restrict__ descs, con
         P.p1 = K.window_base(P.tb - 1) + 6;
         float ub = 0.f;
         V2 mass = V2(0.f);
-        K.piece(P, smem, pipe, faulted, L, sc, ub, mass);
+        const CUtensorMap *tm = descs[w.x].tm_on && !(smem_u32(smem) & 127u) ? descs[w.x].tm[step_s & 1ULL] : nullptr;
+        K.piece(P, smem, pipe, faulted, L, sc, ub, mass, tm);
         const float m = mass.v.x + mass.v.y;
         if (!isfinite(m)) K.ctrl->nonfinite = 1u;
         end_of_step<LY::NT>(K.ctrl, K.k, K.tc.n, (double)ub, (double)m, true, K.mass_on != 0, (unsigned)(nt*ns));
@@ -711,6 +755,9 @@ cudaError_t launch_p(const StepLaunch &L) {
     K.rho_out = (float *)L.macros[0]; K.u_out = (float *)L.macros[1];
     K.v_out = (float *)L.macros[2]; K.w_out = (float *)L.macros[3];
     K.macros_on = L.macros_on; K.mass_on = L.mass;
+    PairTM T;
+    std::memset((void *)&T, 0, sizeof(T));
+    if (L.pmaps) std::memcpy((void *)T.m, L.pmaps, sizeof(T.m));
     static bool attr_done = false;   // one attribute call per instantiation
     constexpr size_t smem = PLay<S, NXC>::smem_bytes;
     if (!attr_done) {
@@ -718,7 +765,7 @@ cudaError_t launch_p(const StepLaunch &L) {
         if (e != cudaSuccess) return e;
         attr_done = true;
     }
-    step_pair_kernel<S, LES, NXC><<<K.tc.grid, PLay<S, NXC>::NT, smem, L.stream>>>(K);
+    step_pair_kernel<S, LES, NXC><<<K.tc.grid, PLay<S, NXC>::NT, smem, L.stream>>>(K, T, L.pmaps != nullptr);
     return cudaGetLastError();
 }
 
@@ -767,6 +814,13 @@ struct PairBatchOps {
         d.buf[0] = (S *)buf0; d.buf[1] = (S *)buf1;
         d.ntiles = ntiles;
         d.nseg = nseg;
+        PairMaps pm;
+        void *const bufs[2] = {buf0, buf1};
+        const char *cp = std::getenv("ISLBM_PAIR_COPIES");
+        if (!(cp && std::strcmp(cp, "bulk") == 0) && make_pair_maps(k, (int)sizeof(S), bufs, &pm)) {
+            std::memcpy((void *)d.tm, (const void *)pm.m, sizeof(d.tm));
+            d.tm_on = 1;
+        }
         std::memcpy(out, (const void *)&d, sizeof(d));
     }
     static cudaError_t prepare() {
@@ -870,6 +924,38 @@ int make_pair_const(const StepConst &k, int precision, const double *wx0, const 
     tc.grid = std::min(tiles*tc.zsegs, slots);
     *out = tc;
     return tc.smem_bytes <= 227*1024 ? 0 : -1;
+}
+
+bool make_pair_maps(const StepConst &k, int elem_bytes, void *const buf[2], PairMaps *out) {
+    out->ok = false;
+    if ((elem_bytes != 4 && elem_bytes != 2) || k.NX > 256 || !pair_supported(k, elem_bytes == 4 ? ISLBM_FP32 : ISLBM_FP16_DEV))
+        return false;
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return false;
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    const int TY = 256/k.NX;   // rows per tile of the paired layout (128 threads, two nodes each)
+    const size_t es = (size_t)elem_bytes;
+    const cuuint64_t dims[4] = {(cuuint64_t)k.NX, (cuuint64_t)k.NY, (cuuint64_t)k.NZ, 19};
+    const cuuint64_t strides[3] = {k.NX*es, (size_t)k.NX*k.NY*es, (size_t)k.NX*k.NY*k.NZ*es};
+    const cuuint32_t boxes[4][4] = {{(cuuint32_t)k.NX, (cuuint32_t)TY + 6, 1, 2}, {(cuuint32_t)k.NX, (cuuint32_t)TY + 6, 1, 4},
+                                    {(cuuint32_t)k.NX, (cuuint32_t)TY, 1, 2}, {(cuuint32_t)k.NX, (cuuint32_t)TY, 1, 4}};
+    const cuuint32_t unit[4] = {1, 1, 1, 1};
+    const CUtensorMapDataType dt = elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT16;
+    for (int b = 0; b < 2; b++)
+        for (int j = 0; j < 4; j++)
+            if (encode(&out->m[b][j], dt, 4, buf[b], dims, strides, boxes[j], unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+                return false;
+    out->buf[0] = buf[0];
+    out->buf[1] = buf[1];
+    out->ok = true;
+    return true;
 }
 
 cudaError_t launch_step_pair(const StepLaunch &L) {

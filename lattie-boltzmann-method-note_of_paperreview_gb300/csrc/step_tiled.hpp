@@ -3,6 +3,7 @@
 
 #include <stddef.h>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "step_common.cuh"
@@ -46,6 +47,23 @@ int make_pair_const(const StepConst &k, int precision, const double *wx0, const 
                     const double *wy2, int num_sms, TiledConst *out);
 int pair_zsegs(int tiles, int slots, int NZ);
 cudaError_t launch_step_pair(const StepLaunch &L);
+// Tensor maps of a solve's two population buffers for the paired kernel's plane copies, one per
+// box shape (m[b][j]: buffer buf[b]; box j = NX x (TY + 6) rows x 2 or 4 populations, NX x TY
+// rows x 2 or 4 populations); ok is false where they are not used (NX > 256, or the driver refused
+// them), and the kernel then copies row runs with cp.async.bulk. A launch takes the maps whose
+// buffer it reads (`for_buffer`), so swapping a handle's buffers cannot pair a map with the
+// wrong one.
+struct PairMaps {
+    CUtensorMap m[2][4];
+    const void *buf[2] = {nullptr, nullptr};
+    bool ok = false;
+    const void *for_buffer(const void *fo) const {
+        for (int b = 0; b < 2; b++)
+            if (ok && buf[b] == fo) return (const void *)m[b];
+        return nullptr;
+    }
+};
+bool make_pair_maps(const StepConst &k, int elem_bytes, void *const buf[2], PairMaps *out);
 size_t pair_batch_desc_bytes(int precision, int NX, bool les);
 void fill_pair_batch_desc(int precision, int NX, bool les, const Tables<float> &T, const StepConst &k, const TiledConst &tc,
                           Ctrl *ctrl, void *const macros[4], void *buf0, void *buf1, int ntiles, int nseg, void *out);

@@ -246,6 +246,24 @@ def test_paired_matches_single_node_kernel(islbm_lib, prec, tol, nx):
     assert abs(b["force"] - a["force"]) <= 1e-3 * abs(a["force"])
 
 
+@pytest.mark.parametrize("prec", ["fp32", "fp16"])
+@pytest.mark.parametrize("nx", [32, 128, 256])
+def test_paired_copy_paths_agree(islbm_lib, monkeypatch, prec, nx):
+    """The paired kernel's two ways of staging a plane, tensor-map boxes (several populations and
+    halo rows per copy) and row-run bulk copies (ISLBM_PAIR_COPIES=bulk; also the path of the
+    tiles whose halo wraps around the streamwise period), deliver the same bytes: the steps agree
+    bit for bit (test_checkpoint's exact resume covers the maps after a buffer swap)."""
+    steps = 23
+    re = re_for_tau(0.6 if nx <= 64 else 0.9, 48)
+    kw = dict(NX=nx, NY=32, NZ=48, NDTFRC=10, precision=prec, Re=re, les_cs=0.1, mass_interval=7, kernel=2)
+    maps = solve(islbm_lib, steps, **kw)
+    monkeypatch.setenv("ISLBM_PAIR_COPIES", "bulk")
+    bulk = solve(islbm_lib, steps, **kw)
+    monkeypatch.delenv("ISLBM_PAIR_COPIES")
+    np.testing.assert_array_equal(maps["f"], bulk["f"])
+    assert maps["force"] == bulk["force"]
+
+
 @pytest.mark.parametrize("prec,tol", [("fp32", 2e-6), ("fp16", 2e-3)])
 def test_tiled_384_tall_grid_vs_gather(islbm_lib, prec, tol):
     """The 384-wide layout of the large benchmark grid on a tall column (NZ = 192, the benchmark
