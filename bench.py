@@ -35,8 +35,8 @@ for _p in (ROOT, PKG):
 
 METRIC = "ISLBM MLUPS & %HBM peak, mixed vs plain FP32 at stated err; serve p50/p99"
 # DRAM bytes of one launch of the FP32 step on this workload, from an ncu capture of the same
-# kernel (dram__bytes_read.sum + dram__bytes_write.sum: 590.3 MB + 433.0 MB)
-NCU_TRAFFIC_BYTES = 1023.3e6
+# kernel (dram__bytes_read.sum + dram__bytes_write.sum: 590.6 MB + 433.0 MB)
+NCU_TRAFFIC_BYTES = 1023.6e6
 CASE = dict(NX=128, NY=256, NZ=192, Re=2800.0, Uref=0.05, NDTFRC=100, les_cs=0.1)
 WORKLOAD = "periodic hill 256x128x192 (streamwise x spanwise x wall-normal), Re_h 2800, LES Cs 0.1, Ub 0.05"
 

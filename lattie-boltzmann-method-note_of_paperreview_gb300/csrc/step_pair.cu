@@ -5,13 +5,15 @@
 // BF16 population storage. Organisation:
 //   * a CTA of 128 threads owns a tile of TY = 256/NX full-width rows (two nodes per thread:
 //     x0 = 2*(thread % (NX/2)) and x0 + 1) and marches upward through a wall-normal segment of
-//     that column; each plane's 18 moving populations are copied global -> shared memory by
-//     cp.async.bulk (the ten with e_y != 0 with a 3-row streamwise halo on both sides, periodic
-//     wrap by splitting the copy); every operand of a copy is uniform over the CTA, so one
-//     thread issues it with a few uniform instructions. An issuing thread stalls for about 50
-//     cycles per copy, so the front copies are issued by thread 0 and the stage copies by
-//     thread 64 (another warp, of the other tile row where a tile has two): the two stalls
-//     overlap (4% faster than one issuer; splitting the front copies as well was slower);
+//     that column; each plane's 18 moving populations are copied global -> shared memory (the
+//     ten with e_y != 0 with a 3-row streamwise halo on both sides) as 4D tensor-map boxes
+//     (cp.async.bulk.tensor: full rows x halo rows x 2 or 4 consecutive populations per copy;
+//     tiles whose halo wraps around the period, and NX = 384, copy row runs with
+//     cp.async.bulk). Every operand of a copy is uniform over the CTA, so one thread issues it
+//     with a few uniform instructions, but the issuing thread stalls for about 50 cycles per
+//     copy: hence few, large copies, the front ones issued by thread 0 and the stage ones by
+//     thread 64 (another warp, of the other tile row where a tile has two), so that the two
+//     stalls overlap (splitting the front copies as well was slower);
 //   * front buffer (populations read before the plane's CTA barrier: the streamwise-filtered
 //     ten and the xi-only 5, 6) and stage buffer (1, 2, 11..14, read after it, plus the target
 //     row's xi weights and f0) have mbarriers of their own, so the front copies of plane p + 2
