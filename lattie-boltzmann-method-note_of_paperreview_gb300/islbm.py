@@ -152,7 +152,7 @@ def default_params(**overrides):
     return p
 
 
-def baseline_params(case, **overrides):
+def benchmark_params(case, **overrides):
     """Parameter sets of the benchmark cases (grid given streamwise x spanwise x wall-normal
     in the benchmark's naming, i.e. NY x NX x NZ here)."""
     cases = {

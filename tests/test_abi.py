@@ -44,7 +44,7 @@ def test_null_handle_is_error(islbm_lib):
 def test_required_bytes_scales_with_precision(islbm_lib):
     sizes = {}
     for prec in ["fp64", "fp32", "fp16", "bf16"]:
-        p = islbm_lib.baseline_params("hill256", precision=prec)
+        p = islbm_lib.benchmark_params("hill256", precision=prec)
         sizes[prec] = islbm_lib.required_bytes(p)
     n = 128 * 256 * 192
     assert sizes["fp32"] >= 2 * 19 * n * 4
@@ -53,7 +53,7 @@ def test_required_bytes_scales_with_precision(islbm_lib):
 
 
 def test_hbm_budget_refusal(islbm_lib):
-    p = islbm_lib.baseline_params("hill256", precision="fp32", hbm_budget_bytes=1 << 20)
+    p = islbm_lib.benchmark_params("hill256", precision="fp32", hbm_budget_bytes=1 << 20)
     with pytest.raises(islbm_lib.IslbmError) as e:
         islbm_lib.Solver(p)
     assert e.value.status == 4
