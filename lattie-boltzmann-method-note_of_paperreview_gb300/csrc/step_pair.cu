@@ -932,15 +932,16 @@ bool make_pair_maps(const StepConst &k, int elem_bytes, void *const buf[2], Pair
     out->ok = false;
     if ((elem_bytes != 4 && elem_bytes != 2) || k.NX > 256 || !pair_supported(k, elem_bytes == 4 ? ISLBM_FP32 : ISLBM_FP16_DEV))
         return false;
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-    if (!encode) {
+    // the driver's encoder, looked up once (thread-safe static initialisation)
+    static const PFN_cuTensorMapEncodeTiled_v12000 encode = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
         void *fn = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess || !fn)
-            return false;
-        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
-    }
+            q != cudaDriverEntryPointSuccess)
+            return nullptr;
+        return (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }();
+    if (!encode) return false;
     const int TY = 256/k.NX;   // rows per tile of the paired layout (128 threads, two nodes each)
     const size_t es = (size_t)elem_bytes;
     const cuuint64_t dims[4] = {(cuuint64_t)k.NX, (cuuint64_t)k.NY, (cuuint64_t)k.NZ, 19};
