@@ -247,7 +247,7 @@ def test_paired_matches_single_node_kernel(islbm_lib, prec, tol, nx):
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp16"])
-@pytest.mark.parametrize("nx", [32, 128, 256])
+@pytest.mark.parametrize("nx", [32, 64, 128, 256])
 def test_paired_copy_paths_agree(islbm_lib, monkeypatch, prec, nx):
     """The paired kernel's two ways of staging a plane, tensor-map boxes (several populations and
     halo rows per copy) and row-run bulk copies (ISLBM_PAIR_COPIES=bulk; also the path of the
