@@ -3,7 +3,8 @@
 //
 // Same step as stream_collide (C/evolution.h:358-684) for FP32 arithmetic with FP32, FP16 or
 // BF16 population storage. Organisation:
-//   * a CTA of 128 threads owns a tile of TY = 256/NX full-width rows (two nodes per thread:
+//   * a CTA of 128 threads owns a tile of TY = 256/NX full-width rows (192 threads and one row
+//     at NX = 384; two nodes per thread:
 //     x0 = 2*(thread % (NX/2)) and x0 + 1) and marches upward through a wall-normal segment of
 //     that column; each plane's 18 moving populations are copied global -> shared memory (the
 //     ten with e_y != 0 with a 3-row streamwise halo on both sides) as 4D tensor-map boxes
@@ -28,7 +29,7 @@
 //     weights stored as duplicated pairs;
 //   * the collision of the pair runs in packed FP32x2 arithmetic (collide_x2), results are
 //     stored as node pairs (8-byte stores for FP32, 4-byte for FP16/BF16);
-//   * persistent CTAs, two per SM (TMEM bound), work items (wall-normal segment, tile) taken
+//   * persistent CTAs, two per SM (one at NX = 384; TMEM bound), work items (wall-normal segment, tile) taken
 //     segment-major so that CTAs running together share their halo rows through L2.
 #include <algorithm>
 #include <cstdlib>
