@@ -37,3 +37,20 @@ def test_single_rank_is_identity():
     sys.path.insert(0, ROOT)
     import bench
     assert bench.slowest_rank_ms(7.5, 1, "cpu") == 7.5
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference: the CPU restatement of the reference step on the benchmark
+    workload, one JSON line whose step counts are the ones timed."""
+    import json
+    import subprocess
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "MLUPS" and line["higher_is_better"] is True
+    assert line["steps"] == 1 and line["warmup"] == 0 and line["value"] > 0
+    assert line["config"]["workload"].startswith("periodic hill 256x128x192")
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["steps"] == 1 and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
